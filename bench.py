@@ -1,0 +1,406 @@
+"""Benchmark: Hex8 linear-elastic Hessian-vector product on a 128^3 brick.
+
+Workload (the reference's Hex8 configuration): structured Hex8 brick 128x128x128
+(2,097,152 elements, 2,146,689 nodes, 6,440,067 dofs), 2x2x2 Gauss, E = 1.0,
+nu = 0.3, clamped x = 0 face, uniform normal traction 1e-3 on x = 1.
+
+* step: one matrix-free HVP y = K v over the whole mesh (FP32 kernel, FP32
+  vectors and coordinates), inputs resident in HBM; the L2 is flushed (256 MiB
+  write) before every step and the HVP is timed with CUDA events on its stream.
+* value: dofs per second (GDOF/s) over the K timed steps, summed over ranks.
+* e2e: the same HVP through the public API with the input copied from pinned host
+  memory and the result copied back inside the timed region.
+* solve: the Jacobi-CG solve of the same problem to true FP64 relative residual
+  1e-10, plain FP64 vs mixed FP32/FP64 (iterative refinement); solves/s of each.
+* roofline: algorithmic bytes per HVP (x read + y written + int32 connectivity +
+  coordinates: 2*4*N_dof + 4*8*E + 4*3*N_nodes = 144.39 MB) over the measured HVP
+  time, against the measured HBM copy bandwidth.
+* cpu_baseline: the numpy restatement (oracle) of the same HVP on a 32^3 brick.
+
+Multi-GPU: replicas only (each rank runs the same workload on its own GPU).
+``--impl reference`` times the CPU restatement of the HVP on all host cores
+(the reference itself needs JAX, which is not installable here).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Hex8 HVP GDOF/s"
+UNIT = "GDOF/s"
+N_CELLS = 128
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_from_profile():
+    """Per-launch DRAM bytes of the HVP kernels from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "hex8_hvp_f32_brick.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_hvp_128:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def brick_problem(n, device):
+    import torch
+
+    from tatva_gb300 import Mesh, Operator, element, materials
+
+    mesh = Mesh.brick(n, n, n, device=device)
+    op = Operator(mesh, element.Hexahedron8())
+    en = materials.LinearElastic.from_young(op, 1.0, 0.3)
+    c = mesh.coords_host()
+    nn = c.shape[0]
+    fixed = np.zeros(nn * 3, np.uint8)
+    left = np.where(c[:, 0] == 0.0)[0]
+    for k in range(3):
+        fixed[left * 3 + k] = 1
+    # consistent nodal forces of a uniform traction t = 1e-3 e_x on x = 1
+    b = np.zeros(nn * 3)
+    h = 1.0 / n
+    right = np.where(c[:, 0] == 1.0)[0]
+    jy = np.rint(c[right, 1] / h).astype(int)
+    jz = np.rint(c[right, 2] / h).astype(int)
+    mult = (np.where((jy == 0) | (jy == n), 1, 2) * np.where((jz == 0) | (jz == n), 1, 2))
+    b[right * 3] = 1e-3 * (h * h / 4) * mult
+    return dict(mesh=mesh, op=op, energy=en, fixed=torch.as_tensor(fixed, device=device),
+                b=torch.as_tensor(b, device=device), n_nodes=nn, n_elems=mesh.n_elements)
+
+
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        import tempfile
+
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clocks unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_hvp_sample(n_cells=32, min_seconds=10.0, processes=1):
+    """Oracle (numpy) HVP of the same law on an n^3 brick: GDOF/s on this host."""
+    from oracle import elements as oe
+    from oracle import materials as omat
+    from oracle import mesh as om
+    from oracle import operator as oop
+
+    c, e = om.brick(n_cells, n_cells, n_cells)
+    mu, lm = omat.lame_from_young(1.0, 0.3)
+    law = omat.LinearElastic(mu, lm)
+    v = np.random.default_rng(0).standard_normal(c.shape[0] * 3)
+    if processes > 1:
+        import multiprocessing as mp
+
+        chunks = np.array_split(np.arange(e.shape[0]), processes)
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(processes, initializer=_pool_init, initargs=(c, e, law, v)) as pool:
+            pool.map(_pool_hvp, [chunks[0][:8]] * processes)  # warm the workers
+            reps, t0 = 0, time.perf_counter()
+            while True:
+                parts = pool.map(_pool_hvp, chunks)
+                y = np.sum(parts, axis=0)
+                reps += 1
+                if time.perf_counter() - t0 >= min_seconds:
+                    break
+            dt = (time.perf_counter() - t0) / reps
+    else:
+        op = oop.OracleOperator(c, e, oe.Hexahedron8())
+        omat.hvp(op, law, None, v)
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            y = omat.hvp(op, law, None, v)
+            reps += 1
+            if time.perf_counter() - t0 >= min_seconds:
+                break
+        dt = (time.perf_counter() - t0) / reps
+    del y
+    ndof = c.shape[0] * 3
+    return ndof / dt / 1e9, dt, ndof, reps
+
+
+_POOL = {}
+
+
+def _pool_init(c, e, law, v):
+    _POOL.update(c=c, e=e, law=law, v=v)
+
+
+def _pool_hvp(idx):
+    from oracle import elements as oe
+    from oracle import materials as omat
+    from oracle import operator as oop
+
+    c, e, law, v = _POOL["c"], _POOL["e"], _POOL["law"], _POOL["v"]
+    op = oop.OracleOperator(c, e[idx], oe.Hexahedron8())
+    return omat.hvp(op, law, None, v)
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n = 48
+    vals = []
+    for _ in range(args.warmup):
+        cpu_hvp_sample(n, min_seconds=0.0, processes=cores)
+    for _ in range(args.steps):
+        g, dt, ndof, reps = cpu_hvp_sample(n, min_seconds=0.0, processes=cores)
+        vals.append(g)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ndof / value / 1e6,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"hex8 linear-elastic HVP, brick {n}^3 sample of the 128^3 brick "
+                               "(E=1, nu=0.3)", "l2": "host CPU"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"numpy restatement of the HVP on a {n}^3 brick "
+                                   f"({ndof} dofs), elements split over {cores} processes"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (JAX) cannot be installed offline; its CPU path is "
+                "represented by the numpy restatement of the same HVP",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    from tatva_gb300 import _lib, autotune, solvers
+    from tatva_gb300._device import ptr
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    P = brick_problem(args.size, dev)
+    en = P["energy"]
+    ndof = en.n_dofs
+    tune = autotune.tune(en, dtype=torch.float32) if args.autotune else None
+    plan = en.plan()
+    g = torch.Generator(device=dev).manual_seed(1234 + rank)
+    v = torch.randn(ndof, dtype=torch.float32, device=dev, generator=g)
+    y = torch.empty_like(v)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream()
+
+    def hvp_step(vv, out):
+        en.apply(_lib.TG_MODE_HVP, None, vv, out=out)
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        hvp_step(v, y)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            evs[i][0].record(st)
+            hvp_step(v, y)
+            evs[i][1].record(st)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    ms_step = float(np.mean(ms))
+    if ws > 1:
+        t = torch.tensor([ms_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = ws * ndof / (ms_step * 1e-3) / 1e9
+
+    # ---- e2e through the public API with host buffers
+    vh = torch.empty(ndof, dtype=torch.float32, pin_memory=True)
+    vh.copy_(v.cpu())
+    yh = torch.empty(ndof, dtype=torch.float32, pin_memory=True)
+    for _ in range(max(1, args.warmup)):
+        yh.copy_(en.hvp(None, vh.to(dev, non_blocking=True)), non_blocking=True)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(st)
+    for _ in range(args.steps):
+        yh.copy_(en.hvp(None, vh.to(dev, non_blocking=True)), non_blocking=True)
+    e.record(st)
+    torch.cuda.synchronize()
+    e2e_ms = s.elapsed_time(e) / args.steps
+    e2e_value = ws * ndof / (e2e_ms * 1e-3) / 1e9
+
+    # ---- roofline of the HVP
+    nn, ne = P["n_nodes"], P["n_elems"]
+    alg_bytes = 2 * 4 * ndof + 4 * 8 * ne + 4 * 3 * nn
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    traffic = _traffic_from_profile() if args.size == N_CELLS else None
+
+    # ---- FP64 HVP and the solves (rank 0 only reports)
+    y64 = torch.empty(ndof, dtype=torch.float64, device=dev)
+    v64 = v.double()
+    for _ in range(2):
+        en.apply(_lib.TG_MODE_HVP, None, v64, out=y64)
+    s.record(st)
+    for _ in range(5):
+        en.apply(_lib.TG_MODE_HVP, None, v64, out=y64)
+    e.record(st)
+    torch.cuda.synchronize()
+    ms64 = s.elapsed_time(e) / 5
+    solve = None
+    if args.solve:
+        b, fixed = P["b"], P["fixed"]
+        r64 = solvers.cg(en, b, fixed=fixed, rtol=1e-10, maxiter=args.max_iter,
+                         check_every=100, raise_on_fail=False)
+        rmx = solvers.mixed_cg(en, b, fixed=fixed, rtol=1e-10, inner_rtol=args.inner_rtol,
+                               max_inner=args.max_iter, check_every=100, raise_on_fail=False)
+        solve = {
+            "rtol": 1e-10,
+            "fp64": {"seconds": r64.seconds, "iterations": r64.iterations,
+                     "rel_res": r64.rel_res, "converged": r64.converged,
+                     "solves_per_s": 1.0 / r64.seconds},
+            "mixed": {"seconds": rmx.seconds, "inner_iterations": rmx.iterations,
+                      "refinements": rmx.outer, "rel_res": rmx.rel_res,
+                      "converged": rmx.converged, "solves_per_s": 1.0 / rmx.seconds},
+            "speedup_mixed_vs_fp64": r64.seconds / rmx.seconds,
+        }
+    if ws > 1:
+        torch.distributed.barrier()
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        gc, dtc, ndc, reps = cpu_hvp_sample(32, min_seconds=args.cpu_seconds, processes=1)
+        cpu = {"value": gc, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"numpy restatement (FP64) of the HVP on a 32^3 brick ({ndc} dofs), "
+                         f"{reps} repetitions, {dtc * 1e3:.1f} ms each"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"hex8 linear-elastic HVP, structured brick {args.size}^3 "
+                               f"({ne} elements, {ndof} dofs), E=1 nu=0.3, 2x2x2 Gauss",
+                   "l2": "flushed before every step (256 MiB write)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "plan": {k: plan.stats()[k] for k in ("block_elems", "threads", "n_blocks",
+                                                          "shared_fraction")}},
+        "gpu_launches": args.steps * (2 if plan.sizes["n_shared"] > 0 else 1),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ndof * 4,
+                "d2h_bytes_per_step": ndof * 4, "ms_per_step": e2e_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind, "algorithmic_bytes": alg_bytes},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "fp64_hvp": {"ms": ms64, "gdof_s": ndof / (ms64 * 1e-3) / 1e9},
+        "solve": solve,
+        "wall_s_timed_region": wall,
+    }
+    if tune:
+        line["autotune"] = tune
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=N_CELLS)
+    ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--solve", type=int, default=1)
+    ap.add_argument("--max-iter", type=int, default=20000)
+    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,338 @@
+/*
+ * tatva_gb300 -- C ABI of the GB300 (sm_103a) finite-element hot path.
+ *
+ * Plain C: device pointers, sizes, an opaque cudaStream_t passed as void*, and an
+ * int status.  No allocation happens on compute calls: every temporary lives in
+ * caller-provided workspace whose size is reported by a *_workspace_bytes query.
+ * Setup routines marked HOST take host pointers and run on the CPU.
+ *
+ * Each entry point names the reference (smec-ethz/tatva 0.11.1) interface it
+ * replaces.  In the reference these are Python/JAX functions; a JAX host binds
+ * the compute entry points as XLA FFI custom calls (the stream argument is the
+ * XLA stream), a PyTorch host (tatva_gb300 package) binds them through ctypes.
+ *
+ * Conventions
+ *   elem   TG_TRI3 | TG_TET4 | TG_HEX8   (node orders of tatva/element/base.py)
+ *   prec   TG_F32 | TG_F64               (every float buffer of a call has this type)
+ *   nodal arrays are (n_nodes, n_vals) row-major; dof = node*n_vals + comp
+ *   quadrature arrays are (n_elems, n_quad, ...) row-major, reference QP order
+ *   conn is int32 (n_elems, nodes_per_element), as tatva/mesh.py:205
+ */
+#ifndef TATVA_GB300_H
+#define TATVA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define TG_API __attribute__((visibility("default")))
+#else
+#define TG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- status codes (mapped to Python exceptions by the host) ---- */
+enum {
+  TG_OK = 0,
+  TG_ERR_VALUE = 1,         /* ValueError   (tatva/operator.py:143-168)      */
+  TG_ERR_TYPE = 2,          /* TypeError    (tatva/operator.py:156-157)      */
+  TG_ERR_CUDA = 3,          /* RuntimeError                                  */
+  TG_ERR_UNSUPPORTED = 4,   /* NotImplementedError                           */
+  TG_ERR_NOT_CONVERGED = 5, /* solver hit max_iter before the tolerance      */
+  TG_ERR_WORKSPACE = 6,     /* workspace smaller than the *_workspace_bytes  */
+  TG_ERR_BREAKDOWN = 7,     /* CG breakdown (p.Ap <= 0) or non-finite value  */
+};
+
+enum { TG_TRI3 = 0, TG_TET4 = 1, TG_HEX8 = 2 };
+enum { TG_F32 = 0, TG_F64 = 1 };
+enum { TG_POISSON = 0, TG_LINEAR_ELASTIC = 1, TG_NEO_HOOKEAN = 2 };
+enum { TG_MODE_RESIDUAL = 0, TG_MODE_HVP = 1, TG_MODE_DIAG = 2 };
+
+/* last error message of the calling thread ("" if none) */
+TG_API const char* tg_last_error(void);
+TG_API int tg_version(void);
+/* number of SMs of the current device (0 when no device) */
+TG_API int tg_device_sm_count(void);
+
+/* ============================================================================
+ * Operator maps (K1-K3).  Replaces tatva/operator.py Operator.eval (:358-377),
+ * Operator.grad (:379-397), get_integration_weights (:172-192),
+ * _integrate_quad_array (:344-356), integrate (:307-319), and the reverse-mode
+ * transposes of the gather nodal_values[mesh.elements] (:221,256).
+ * ========================================================================== */
+
+/* out (E,Q,V) = sum_a N_a(xi_q) nodal[conn[e,a], :]            operator.py:358-377 */
+TG_API int tg_eval(int elem, int prec, const void* nodal, int64_t n_nodes, int n_vals,
+            const int32_t* conn, int64_t n_elems, void* out, void* stream);
+
+/* out (E,Q,V,D) = grad of nodal at QPs (value dims first, spatial last)
+ *                                                  operator.py:379-397, base.py:99-115 */
+TG_API int tg_grad(int elem, int prec, const void* nodal, const void* coords, int64_t n_nodes,
+            int n_vals, const int32_t* conn, int64_t n_elems, void* out, void* stream);
+
+/* out (E,Q) = detJ * w_q                                        operator.py:172-192 */
+TG_API int tg_integration_weights(int elem, int prec, const void* coords, int64_t n_nodes,
+                           const int32_t* conn, int64_t n_elems, void* out, void* stream);
+
+/* out (E,V) = sum_q quad[e,q,:] * weights[e,q]      ("eq...,eq->e...") operator.py:344-356 */
+TG_API int tg_integrate_quad(int prec, const void* quad, const void* weights, int64_t n_elems,
+                      int n_quad, int n_vals, void* out, void* stream);
+
+/* out (V) = sum over rows of in (R,V): deterministic fixed-order two-stage sum.
+ * Replaces jnp.sum(res, axis=0) of Operator.integrate (operator.py:318-319).     */
+TG_API size_t tg_sum_rows_workspace_bytes(int prec, int n_vals);
+TG_API int tg_sum_rows(int prec, const void* in, int64_t n_rows, int n_vals, void* out,
+                void* workspace, size_t workspace_bytes, void* stream);
+
+/* out (E,n_e,V) = nodal[conn]  (the gather of Operator.map, operator.py:255-258) */
+TG_API int tg_gather_nodal(int prec, const void* nodal, int64_t n_nodes, int n_vals,
+                    const int32_t* conn, int64_t n_elems, int nodes_per_elem, void* out,
+                    void* stream);
+
+/* (E,Q,V) out[e,q,:] = g[e,:] * weights[e,q]: transpose of tg_integrate_quad */
+TG_API int tg_integrate_quad_transpose(int prec, const void* g, const void* weights,
+                                       int64_t n_elems, int n_quad, int n_vals, void* out,
+                                       void* stream);
+/* out (N,V) = sum over incident (e,a) of vals[e,a,:]: transpose of tg_gather_nodal */
+TG_API int tg_scatter_nodal(int prec, const void* vals, int64_t n_nodes, int n_vals,
+                            int nodes_per_elem, const int32_t* inc_ptr, const int32_t* inc_idx,
+                            void* out, void* stream);
+
+/* Transposes (reverse-mode AD of grad / eval; no reference function: the
+ * reference gets them from XLA's transpose of the gather at operator.py:221).
+ * out (N,V) = sum over incident (e,a) of sum_q sum_d dNdX[e,q,d,a] flux[e,q,:,d]
+ * The node->(e*n_e+a) incidence CSR comes from tg_node_incidence (HOST) and fixes
+ * the summation order: the result is deterministic.                            */
+TG_API int tg_grad_transpose(int elem, int prec, const void* flux, const void* coords,
+                      int64_t n_nodes, int n_vals, const int32_t* conn, int64_t n_elems,
+                      const int32_t* inc_ptr, const int32_t* inc_idx, void* out,
+                      void* stream);
+TG_API int tg_eval_transpose(int elem, int prec, const void* quad, int64_t n_nodes, int n_vals,
+                      const int32_t* conn, int64_t n_elems, const int32_t* inc_ptr,
+                      const int32_t* inc_idx, void* out, void* stream);
+
+/* ============================================================================
+ * Fused element assembly (K4 residual, K5 HVP, Jacobi diagonal) over a
+ * deterministic element-block plan.  Replaces jax.grad(E) and
+ * jax.jvp(jax.grad(E)) of the energies on the hot path (README.md:93,
+ * tatva/sparse/base.py:257-265): Poisson 1/2 kappa|grad u|^2 - f u, linear
+ * elastic 1/2 sigma:eps, Neo-Hookean mu/2(I1-3-2lnJ)+lambda/2(lnJ)^2
+ * (tests/test_sparse_tracer.py:101-113).
+ * ========================================================================== */
+
+/* Element-block plan: elements grouped into spatially compact blocks; each block
+ * stages its nodes in shared memory, accumulates element results in block-local
+ * element-colour order, writes nodes it owns alone and leaves partial sums for
+ * nodes shared with other blocks, which a second pass adds in fixed order.   */
+typedef struct tg_block_plan {
+  int32_t n_blocks;
+  int32_t n_elems;
+  int32_t nodes_per_elem_padded; /* stride of lconn (4 for Tri3/Tet4, 8 for Hex8) */
+  int32_t max_local_nodes;       /* shared-memory sizing                          */
+  int32_t n_shared;              /* nodes touched by more than one block          */
+  int32_t n_partials;            /* partial-sum slots                             */
+  int32_t threads;               /* threads per block (64/128/256; 0 = 256)       */
+  int32_t reserved;
+  const int32_t* blk_elem_ptr;   /* [n_blocks+1] element range of block b         */
+  const int32_t* blk_color_ptr;  /* [n_blocks+1] range of b's entries in color_ofs*/
+  const int32_t* color_ofs;      /* per block: colour boundaries, relative         */
+  const int32_t* blk_node_ptr;   /* [n_blocks+1] range of b's local nodes          */
+  const uint16_t* lconn;         /* [n_elems*stride] block-local connectivity      */
+  const int32_t* elem_id;        /* [n_elems] original element id                  */
+  const int32_t* lnode_gid;      /* [sum L_b] global node id                       */
+  const int32_t* lnode_slot;     /* [sum L_b] -1: owned alone, else partial slot   */
+  const int32_t* shared_node;    /* [n_shared] global node id                      */
+  const int32_t* shared_ptr;     /* [n_shared+1]                                   */
+  const int32_t* shared_slots;   /* [n_partials] slots in summation order          */
+} tg_block_plan;
+
+/* Material parameters.  kind = TG_POISSON: p0 = kappa, p1 = f (source);
+ * TG_LINEAR_ELASTIC: p0 = mu, p1 = lambda; TG_NEO_HOOKEAN: p0 = mu, p1 = lambda.
+ * elem_param (optional, prec-typed, (n_elems,) in ORIGINAL element order) replaces
+ * p0 per element (per-element conductivity through Operator.map's
+ * element_quantity, tatva/operator.py:255-258).                                  */
+typedef struct tg_material {
+  int32_t kind;
+  int32_t reserved;
+  double p0, p1, p2, p3;
+  const void* elem_param;
+} tg_material;
+
+/* HOST: build a plan.  conn/coords are host arrays (coords FP64, dim = 2 or 3).
+ * block_elems: target elements per block; max_local_nodes: cap (<= 65535).   */
+TG_API int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int64_t n_nodes,
+                  const double* coords, int dim, int block_elems, int max_local_nodes,
+                  void** handle);
+/* sizes[0..8] = n_blocks, n_elems, color_ofs_len, total_local_nodes, n_shared,
+ * n_partials, max_local_nodes, max_block_colors, stride                          */
+TG_API int tg_plan_sizes(const void* handle, int64_t* sizes);
+TG_API int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t* blk_color_ptr,
+                   int32_t* color_ofs, int32_t* blk_node_ptr, uint16_t* lconn,
+                   int32_t* elem_id, int32_t* lnode_gid, int32_t* lnode_slot,
+                   int32_t* shared_node, int32_t* shared_ptr, int32_t* shared_slots);
+TG_API void tg_plan_free(void* handle);
+
+/* y = mode(u, v) over the plan:
+ *   RESIDUAL  y = dE/du (u)               v unused
+ *   HVP       y = d2E/du2 (u) . v         u unused for linear laws (may be NULL)
+ *   DIAG      y = diag d2E/du2 (u)        v unused
+ * fixed (optional, (n_nodes*V) uint8): Dirichlet mask with the semantics of
+ * Lifter.reduce_adjoint/Fixed (tatva/lifter/base.py:235-251,
+ * lifter/constraints.py:312-318): inputs v are read as 0 on fixed dofs and the
+ * output on fixed dofs is 0 (RESIDUAL), v (HVP, identity block) or 1 (DIAG).
+ * coords must have precision prec.  Workspace: tg_apply_workspace_bytes.     */
+TG_API size_t tg_apply_workspace_bytes(int elem, int prec, int mat_kind, const tg_block_plan* plan);
+TG_API int tg_apply(int elem, int prec, int mode, const tg_material* mat, const tg_block_plan* plan,
+             const void* coords, int64_t n_nodes, const void* u, const void* v,
+             const uint8_t* fixed, void* y, void* workspace, size_t workspace_bytes,
+             void* stream);
+/* Per-element energies (n_elems,) in original element order (E(u) before the sum). */
+TG_API int tg_energy_per_element(int elem, int prec, const tg_material* mat, const void* coords,
+                          int64_t n_nodes, const int32_t* conn, int64_t n_elems,
+                          const void* u, void* out, void* stream);
+
+/* ============================================================================
+ * Colored compressed Hessian (K6) and CSR decompression.  Replaces
+ * tatva/sparse/base.py compute_rows_cols (:108-136), colored_jacobian_batch
+ * (:230-270) and the decompression data = Jc[rows, col_colors] of jacfwd /
+ * linearized_jacfwd (:173, :224).
+ * ========================================================================== */
+
+/* Jc (n_nodes*V, n_colors) row-major, overwritten:
+ *   Jc[i, c] = sum_{j : dof_colors[j] == c} H[i, j],  H = d2E/du2(u)
+ * computed from element tangents, accumulated in element-colour order
+ * (elem_order/elem_color_ptr from tg_element_colors; elem_color_ptr is HOST). */
+TG_API int tg_compressed_hessian(int elem, int prec, const tg_material* mat, const void* coords,
+                          int64_t n_nodes, const int32_t* conn, int64_t n_elems,
+                          const void* u, const int32_t* elem_order,
+                          const int32_t* elem_color_ptr_host, int n_elem_colors,
+                          const int32_t* dof_colors, int n_colors, void* Jc, void* stream);
+/* rows[k] = row of nonzero k; col_colors[k] = colors[indices[k]]   base.py:108-136 */
+TG_API int tg_rows_cols(const int32_t* indptr, const int32_t* indices, const int32_t* colors,
+                 int64_t n_rows, int64_t nnz, int32_t* rows, int32_t* col_colors,
+                 void* stream);
+/* data[k] = Jc[rows[k], col_colors[k]]                              base.py:173 */
+TG_API int tg_decompress(int prec, const void* Jc, int n_colors, const int32_t* rows,
+                  const int32_t* col_colors, int64_t nnz, void* data, void* stream);
+/* seeds (nc, n): seeds[j, i] = (colors[i] == c0 + j) ? 1 : 0         base.py:259 */
+TG_API int tg_color_seeds(int prec, const int32_t* colors, int64_t n, int c0, int nc, void* seeds,
+                   void* stream);
+/* Jc[:, c] = col  (assemble one compressed column from a JVP)      base.py:268-270 */
+TG_API int tg_set_column(int prec, const void* col, int64_t n, int n_colors, int c, void* Jc,
+                  void* stream);
+
+/* ============================================================================
+ * Sparse / vector kernels (K7, K8) for solvers composed on top of the path
+ * (the reference has no solver; users call jax.scipy.sparse.linalg.cg).
+ * ========================================================================== */
+
+/* y = A x, CSR (int32 indptr/indices), data/x/y of precision prec */
+TG_API int tg_spmv(int prec, int64_t n_rows, const int32_t* indptr, const int32_t* indices,
+            const void* data, const void* x, void* y, void* stream);
+/* CSR diagonal (Jacobi) */
+TG_API int tg_csr_diagonal(int prec, int64_t n_rows, const int32_t* indptr, const int32_t* indices,
+                    const void* data, void* diag, void* stream);
+/* out_dev[0] = sum x_i y_i accumulated in FP64, deterministic (fixed partition
+ * and tree order independent of the GPU).  out_dev is a device double.        */
+TG_API size_t tg_dot_workspace_bytes(void);
+TG_API int tg_dot(int prec, const void* x, const void* y, int64_t n, double* out_dev,
+           void* workspace, size_t workspace_bytes, void* stream);
+/* y = a*x + b*y (a, b host doubles) */
+TG_API int tg_axpby(int prec, int64_t n, double a, const void* x, double b, void* y, void* stream);
+/* out = in converted to prec_out */
+TG_API int tg_convert(int prec_in, const void* in, int prec_out, void* out, int64_t n, void* stream);
+
+/* Solver statistics (filled by the solve entry points). */
+typedef struct tg_solve_stats {
+  int32_t status;       /* TG_OK / TG_ERR_NOT_CONVERGED / TG_ERR_BREAKDOWN */
+  int32_t iterations;   /* total (inner) CG iterations                      */
+  int32_t outer;        /* refinement steps (mixed solve)                   */
+  int32_t reserved;
+  double rel_res;       /* final FP64 true relative residual ||b-Ax||/||b|| */
+} tg_solve_stats;
+
+/* Description of an operator A: either matrix-free, A = d2E/du2(u) restricted by
+ * the Dirichlet mask (tg_apply in HVP mode), or, when csr_data != NULL, an
+ * assembled CSR matrix of n_rows rows (Dirichlet rows/columns already applied
+ * with tg_csr_apply_dirichlet).                                              */
+typedef struct tg_operator_desc {
+  int32_t elem;
+  int32_t prec;
+  tg_material mat;
+  const tg_block_plan* plan;
+  const void* coords;    /* precision prec */
+  int64_t n_nodes;
+  const void* u;         /* linearisation point (nonlinear laws), precision prec */
+  const uint8_t* fixed;  /* Dirichlet mask or NULL */
+  int64_t n_rows;
+  const int32_t* csr_indptr;
+  const int32_t* csr_indices;
+  const void* csr_data;  /* precision prec */
+} tg_operator_desc;
+
+/* Dirichlet rows/columns of an assembled matrix: for fixed rows data = (col == row);
+ * entries in fixed columns of free rows are zeroed.                          */
+TG_API int tg_csr_apply_dirichlet(int prec, int64_t n_rows, const int32_t* indptr,
+                           const int32_t* indices, const uint8_t* fixed, void* data,
+                           void* stream);
+/* y = A x for an operator description (one HVP or SpMV).                    */
+TG_API size_t tg_operator_workspace_bytes(const tg_operator_desc* op);
+TG_API int tg_operator_apply(const tg_operator_desc* op, const void* x, void* y, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* Jacobi-preconditioned CG, all vectors of precision op->prec, scalars and dot
+ * products in FP64 on the device.  Solves A x = b from the given x.  The loop runs
+ * `check_every` iterations per CUDA graph replay between host convergence checks
+ * and never exceeds max_iter.                                                  */
+TG_API size_t tg_cg_workspace_bytes(const tg_operator_desc* op);
+TG_API int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, const void* diag,
+                double rtol, int max_iter, int check_every, void* workspace,
+                size_t workspace_bytes, tg_solve_stats* stats, void* stream);
+
+/* Mixed precision: FP32 Jacobi-CG inner solves on op32 (FP32 HVP, FP64 dots),
+ * FP64 iterative refinement with the true residual r = b - A64 x on op64.
+ * b, x, diag64 are FP64; converges to ||b - A64 x|| <= rtol ||b||.           */
+TG_API size_t tg_mixed_workspace_bytes(const tg_operator_desc* op64, const tg_operator_desc* op32);
+TG_API int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_desc* op32,
+                   const double* b, double* x, const double* diag64, double rtol,
+                   double inner_rtol, int max_outer, int max_inner, int check_every,
+                   void* workspace, size_t workspace_bytes, tg_solve_stats* stats,
+                   void* stream);
+
+/* ============================================================================
+ * HOST setup (H1).  Replaces tatva/sparse/_extraction.py _create_sparse_structure
+ * / pattern_from_mesh (:37-102), tatva_coloring.distance2_colors as restated by
+ * tatva/sparse/_coloring.py (:27-48, :136-153, :270-283).
+ * ========================================================================== */
+
+/* CSR pattern of the dof-level matrix, identical (bit-exact) to
+ * _create_sparse_structure: rows/cols sorted, dof = node*ndpn + comp.        */
+TG_API int tg_pattern_build(const int32_t* conn, int64_t n_elems, int nodes_per_elem,
+                     int64_t n_nodes, int n_dofs_per_node, void** handle);
+TG_API int tg_pattern_nnz(const void* handle, int64_t* nnz);
+TG_API int tg_pattern_export(const void* handle, int32_t* indptr, int32_t* indices);
+TG_API void tg_pattern_free(void* handle);
+
+/* Natural-order greedy distance-2 colouring of the CSR pattern (A @ A
+ * neighbourhoods; smallest unused colour), bit-exact with
+ * tatva/sparse/_coloring.py greedy_coloring(get_distance2_adjacency(...)).    */
+TG_API int tg_distance2_colors(const int32_t* indptr, const int32_t* indices, int64_t n,
+                        int32_t* colors, int32_t* n_colors);
+
+/* Greedy natural-order element colouring (elements sharing a node differ).
+ * order (n_elems): elements sorted by colour (stable); color_ptr (<= 129).   */
+TG_API int tg_element_colors(const int32_t* conn, int64_t n_elems, int nodes_per_elem,
+                      int64_t n_nodes, int32_t* colors, int32_t* order,
+                      int32_t* color_ptr, int32_t* n_colors);
+
+/* node -> (e*nodes_per_elem + a) incidence CSR, entries in increasing e.    */
+TG_API int tg_node_incidence(const int32_t* conn, int64_t n_elems, int nodes_per_elem,
+                      int64_t n_nodes, int32_t* ptr, int32_t* idx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TATVA_GB300_H */

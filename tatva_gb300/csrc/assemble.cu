@@ -1,0 +1,631 @@
+// Fused element assembly over an element-block plan: residual (K4), Hessian-vector
+// product (K5) and Jacobi diagonal, for Tri3 / Tet4 / Hex8 and the Poisson, linear
+// elastic and Neo-Hookean laws, in FP32 or FP64.
+//
+// Reference semantics: y = jax.grad(E)(u) and y = jax.jvp(jax.grad(E), (u,), (v,))[1]
+// for E(u) = op.integrate(psi(op.grad(u))) (README.md:93, tatva/sparse/base.py:257-265),
+// i.e. gather (operator.py:221) -> per-QP law -> scatter-add (XLA's transpose of the
+// gather).
+//
+// Determinism without float atomics: every CTA owns one block of spatially compact
+// elements, stages the block's nodes in shared memory, processes its elements colour
+// by colour (no two elements of a colour share a node, so the shared-memory adds do
+// not race), then writes the nodes it owns alone straight to y and the nodes shared
+// with other blocks to partial-sum slots.  A second kernel adds each shared node's
+// partials in the fixed slot order.  The summation order is fixed by the plan, so
+// the result is bitwise reproducible.
+//
+// Hex8 fast path: for an affine (parallelepiped) element and a law that is quadratic
+// in grad u (linear elasticity, Poisson), the 2x2x2 Gauss sum is evaluated exactly in
+// the orthogonal monomial basis {1, x, y, z, yz, xz, xy} of grad u: the nodal values
+// are taken to modal coefficients with an 8-point Walsh-Hadamard transform, the law is
+// applied once per monomial (with the Gauss weight sum_q M(xi_q)^2 of that monomial),
+// and the result returns through the transposed transform.  The Gauss rule integrates these
+// products exactly, so the result equals the per-QP evaluation up to rounding, at
+// roughly 1/8 of the flops.  Non-affine elements take the per-QP path.
+#include "tg_common.cuh"
+#include "tg_dispatch.cuh"
+#include "tg_materials.cuh"
+
+namespace tg {
+
+constexpr int APPLY_MAX_THREADS = 256;
+
+template <int ET, int MAT>
+struct Supported {
+  static constexpr bool value = !(MAT == TG_NEO_HOOKEAN && Elem<ET>::D != 3);
+};
+
+// ------------------------------------------------------------------ generic per-QP element
+template <int ET, int MAT, class T, int MODE>
+__device__ __forceinline__ void element_generic(
+    const Law<MAT, Elem<ET>::D, T>& law, const T (&X)[Elem<ET>::NN][Elem<ET>::D],
+    const T (&U)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V],
+    const T (&W)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V],
+    T (&Y)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V]) {
+  using E = Elem<ET>;
+  using L = Law<MAT, E::D, T>;
+  constexpr int NN = E::NN, D = E::D, V = L::V;
+#pragma unroll
+  for (int a = 0; a < NN; ++a)
+#pragma unroll
+    for (int i = 0; i < V; ++i) Y[a][i] = T(0);
+#pragma unroll
+  for (int q = 0; q < E::Q; ++q) {
+    T G[NN][D];
+    const T wd = qp_geometry<ET, T>(q, X, G) * E::template w<T>(q);
+    T H[V][D];
+    if constexpr (MODE == TG_MODE_RESIDUAL || !L::LINEAR) {
+#pragma unroll
+      for (int i = 0; i < V; ++i)
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          T s = T(0);
+#pragma unroll
+          for (int a = 0; a < NN; ++a) s += G[a][d] * U[a][i];
+          H[i][d] = s;
+        }
+    }
+    if constexpr (MODE == TG_MODE_RESIDUAL) {
+      T P[V][D];
+      law.flux(H, P);
+#pragma unroll
+      for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          T s = T(0);
+#pragma unroll
+          for (int d = 0; d < D; ++d) s += P[i][d] * G[a][d];
+          Y[a][i] += wd * s;
+        }
+      if constexpr (MAT == TG_POISSON) {
+        const T f = law.source();
+#pragma unroll
+        for (int a = 0; a < NN; ++a) Y[a][0] -= wd * f * E::template N<T>(q, a);
+      }
+    } else if constexpr (MODE == TG_MODE_HVP) {
+      const auto lin = law.linearize(H);
+      T dH[V][D], dP[V][D];
+#pragma unroll
+      for (int i = 0; i < V; ++i)
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          T s = T(0);
+#pragma unroll
+          for (int a = 0; a < NN; ++a) s += G[a][d] * W[a][i];
+          dH[i][d] = s;
+        }
+      lin.dflux(dH, dP);
+#pragma unroll
+      for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          T s = T(0);
+#pragma unroll
+          for (int d = 0; d < D; ++d) s += dP[i][d] * G[a][d];
+          Y[a][i] += wd * s;
+        }
+    } else {  // diagonal of the element tangent
+      const auto lin = law.linearize(H);
+#pragma unroll
+      for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          T dH[V][D], dP[V][D];
+#pragma unroll
+          for (int k = 0; k < V; ++k)
+#pragma unroll
+            for (int d = 0; d < D; ++d) dH[k][d] = (k == i) ? G[a][d] : T(0);
+          lin.dflux(dH, dP);
+          T s = T(0);
+#pragma unroll
+          for (int d = 0; d < D; ++d) s += dP[i][d] * G[a][d];
+          Y[a][i] += wd * s;
+        }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ Hex8 affine modal path
+// node a <-> tensor index t = bx + 2 by + 4 bz (bits of the reference coordinates)
+__host__ __device__ constexpr int hex_t(int a) { return (a == 2) ? 3 : (a == 3) ? 2 : (a == 6) ? 7 : (a == 7) ? 6 : a; }
+
+// in place: m[S] = sum_t v_t prod_{i in S} s_i(t), S = bit set over (x, y, z)
+template <class T>
+__device__ __forceinline__ void hadamard8(T (&m)[8]) {
+#pragma unroll
+  for (int h = 1; h < 8; h <<= 1)
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (!(t & h)) {
+        const T a = m[t], b = m[t | h];
+        m[t] = b + a;
+        m[t | h] = b - a;
+      }
+}
+
+// transpose of hadamard8 (its matrix is not symmetric: entries are products of
+// (2 bit - 1) signs): y_t = sum_S m[S] prod_{i in S} s_i(t)
+template <class T>
+__device__ __forceinline__ void hadamard8_t(T (&m)[8]) {
+#pragma unroll
+  for (int h = 1; h < 8; h <<= 1)
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (!(t & h)) {
+        const T a = m[t], b = m[t | h];
+        m[t] = a - b;
+        m[t | h] = a + b;
+      }
+}
+
+template <class T>
+__device__ __forceinline__ bool hex_affine_geometry(const T (&X)[8][3], T (&R)[3][3], T& detJm) {
+  T Jm[3][3];
+  bool affine = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    T m[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) m[hex_t(a)] = X[a][k];
+    hadamard8(m);
+    Jm[0][k] = m[1];
+    Jm[1][k] = m[2];
+    Jm[2][k] = m[4];
+    affine = affine && (m[3] == T(0)) && (m[5] == T(0)) && (m[6] == T(0)) && (m[7] == T(0));
+  }
+  detJm = inv3(Jm, R);
+  return affine;
+}
+
+// one monomial mode of a vector law: G[i][j] (direction i, component j; only the
+// directions flagged in MASK are non-zero) -> F[j][i] = d psi / d G[i][j], scaled.
+template <class T, int MASK, int V, int MAT>
+__device__ __forceinline__ void modal_flux(const T (&R)[3][3], const T (&G)[3][V], T mu, T lam,
+                                           T (&F)[V][3]) {
+  T H[V][3];
+#pragma unroll
+  for (int j = 0; j < V; ++j)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      T s = T(0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        if (MASK & (1 << i)) s += R[k][i] * G[i][j];
+      H[j][k] = s;
+    }
+  T P[V][3];
+  if constexpr (MAT == TG_LINEAR_ELASTIC) {
+    Law<TG_LINEAR_ELASTIC, 3, T>::stress(mu, lam, H, P);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) P[0][k] = mu * H[0][k];
+  }
+#pragma unroll
+  for (int j = 0; j < V; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (MASK & (1 << i)) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) s += P[j][k] * R[k][i];
+        F[j][i] = s;
+      } else {
+        F[j][i] = T(0);
+      }
+    }
+}
+
+// y = dE/du for psi quadratic in grad u (LE: mu, lam; Poisson: kappa in mu), affine hex.
+// W holds the nodal values the quadratic form acts on.  Returns the element
+// Jacobian determinant (unscaled: det(8 J)).
+template <int MAT, class T>
+__device__ __forceinline__ void hex_modal_apply(const T (&R)[3][3], T detJm, T mu, T lam,
+                                                const T (&W)[8][LawDims<MAT, 3>::V],
+                                                T (&Y)[8][LawDims<MAT, 3>::V]) {
+  constexpr int V = LawDims<MAT, 3>::V;
+  const T g2 = T(HEX_GAUSS) * T(HEX_GAUSS);
+  // detJ * sum_q M(xi_q)^2 for the three monomial classes (w_q = 1, detJ = detJm/512)
+  const T s0 = detJm * T(1.0 / 64);
+  const T s1 = s0 * g2;
+  const T s2 = s1 * g2;
+  T M[V][8];
+#pragma unroll
+  for (int j = 0; j < V; ++j) {
+#pragma unroll
+    for (int a = 0; a < 8; ++a) M[j][hex_t(a)] = W[a][j];
+    hadamard8(M[j]);
+  }
+  T dM[V][8];
+  {
+    T G[3][V], F[V][3];
+#pragma unroll
+    for (int j = 0; j < V; ++j) { G[0][j] = M[j][1]; G[1][j] = M[j][2]; G[2][j] = M[j][4]; }
+    modal_flux<T, 7, V, MAT>(R, G, mu * s0, lam * s0, F);
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      dM[j][0] = T(0);
+      dM[j][1] = F[j][0];
+      dM[j][2] = F[j][1];
+      dM[j][4] = F[j][2];
+    }
+  }
+  {  // monomial x: directions (y, z) carry (M12, M13)
+    T G[3][V], F[V][3];
+#pragma unroll
+    for (int j = 0; j < V; ++j) { G[0][j] = T(0); G[1][j] = M[j][3]; G[2][j] = M[j][5]; }
+    modal_flux<T, 6, V, MAT>(R, G, mu * s1, lam * s1, F);
+#pragma unroll
+    for (int j = 0; j < V; ++j) { dM[j][3] = F[j][1]; dM[j][5] = F[j][2]; }
+  }
+  {  // monomial y: directions (x, z) carry (M12, M23)
+    T G[3][V], F[V][3];
+#pragma unroll
+    for (int j = 0; j < V; ++j) { G[0][j] = M[j][3]; G[1][j] = T(0); G[2][j] = M[j][6]; }
+    modal_flux<T, 5, V, MAT>(R, G, mu * s1, lam * s1, F);
+#pragma unroll
+    for (int j = 0; j < V; ++j) { dM[j][3] += F[j][0]; dM[j][6] = F[j][2]; }
+  }
+  {  // monomial z: directions (x, y) carry (M13, M23)
+    T G[3][V], F[V][3];
+#pragma unroll
+    for (int j = 0; j < V; ++j) { G[0][j] = M[j][5]; G[1][j] = M[j][6]; G[2][j] = T(0); }
+    modal_flux<T, 3, V, MAT>(R, G, mu * s1, lam * s1, F);
+#pragma unroll
+    for (int j = 0; j < V; ++j) { dM[j][5] += F[j][0]; dM[j][6] += F[j][1]; }
+  }
+  {  // monomials yz, xz, xy: direction x, y, z carries M123
+    T G[3][V], F[V][3];
+#pragma unroll
+    for (int j = 0; j < V; ++j) { G[0][j] = M[j][7]; G[1][j] = T(0); G[2][j] = T(0); }
+    modal_flux<T, 1, V, MAT>(R, G, mu * s2, lam * s2, F);
+#pragma unroll
+    for (int j = 0; j < V; ++j) dM[j][7] = F[j][0];
+#pragma unroll
+    for (int j = 0; j < V; ++j) { G[0][j] = T(0); G[1][j] = M[j][7]; }
+    modal_flux<T, 2, V, MAT>(R, G, mu * s2, lam * s2, F);
+#pragma unroll
+    for (int j = 0; j < V; ++j) dM[j][7] += F[j][1];
+#pragma unroll
+    for (int j = 0; j < V; ++j) { G[1][j] = T(0); G[2][j] = M[j][7]; }
+    modal_flux<T, 4, V, MAT>(R, G, mu * s2, lam * s2, F);
+#pragma unroll
+    for (int j = 0; j < V; ++j) dM[j][7] += F[j][2];
+  }
+#pragma unroll
+  for (int j = 0; j < V; ++j) {
+    hadamard8_t(dM[j]);
+#pragma unroll
+    for (int a = 0; a < 8; ++a) Y[a][j] = dM[j][hex_t(a)];
+  }
+}
+
+// ------------------------------------------------------------------ per-element dispatch
+template <int ET, int MAT, class T, int MODE>
+__device__ __forceinline__ void element_apply(
+    T p0, T p1, const T (&X)[Elem<ET>::NN][Elem<ET>::D],
+    const T (&U)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V],
+    const T (&W)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V],
+    T (&Y)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V]) {
+  using E = Elem<ET>;
+  const Law<MAT, E::D, T> law(p0, p1);
+  if constexpr (ET == TG_HEX8 && (MAT == TG_LINEAR_ELASTIC || MAT == TG_POISSON) &&
+                MODE != TG_MODE_DIAG) {
+    T R[3][3], detJm;
+    if (hex_affine_geometry(X, R, detJm)) {
+      const T lam = (MAT == TG_LINEAR_ELASTIC) ? p1 : T(0);
+      if constexpr (MODE == TG_MODE_RESIDUAL) {
+        hex_modal_apply<MAT, T>(R, detJm, p0, lam, U, Y);
+        if constexpr (MAT == TG_POISSON) {
+          // -f int N_a = -f detJ (sum_q N_a(xi_q) = 1 for the 2x2x2 rule)
+          const T fd = p1 * detJm * T(1.0 / 512);
+#pragma unroll
+          for (int a = 0; a < 8; ++a) Y[a][0] -= fd;
+        }
+      } else {
+        hex_modal_apply<MAT, T>(R, detJm, p0, lam, W, Y);
+      }
+      return;
+    }
+  }
+  element_generic<ET, MAT, T, MODE>(law, X, U, W, Y);
+}
+
+// ------------------------------------------------------------------ block kernel
+template <int ET, int MAT, class T, int MODE>
+struct ApplyCfg {
+  using E = Elem<ET>;
+  static constexpr int D = E::D, V = LawDims<MAT, D>::V;
+  static constexpr bool LINEAR = Law<MAT, D, T>::LINEAR;
+  static constexpr bool NEED_U = (MODE == TG_MODE_RESIDUAL) || !LINEAR;
+  static constexpr bool NEED_W = (MODE == TG_MODE_HVP);
+  static constexpr int WORDS_PER_NODE = D + (NEED_U ? V : 0) + (NEED_W ? V : 0) + V;
+};
+
+template <int ET, int MAT, class T, int MODE>
+__global__ void __launch_bounds__(APPLY_MAX_THREADS)
+    block_apply_kernel(const tg_block_plan p, const T* __restrict__ coords,
+                       const T* __restrict__ u, const T* __restrict__ v,
+                       const uint8_t* __restrict__ fixed, T* __restrict__ y,
+                       T* __restrict__ partials, T p0, T p1, const T* __restrict__ eparam) {
+  using C = ApplyCfg<ET, MAT, T, MODE>;
+  using E = Elem<ET>;
+  constexpr int NN = E::NN, D = C::D, V = C::V, NPAD = E::NPAD;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
+
+  const int b = blockIdx.x;
+  const int n0 = p.blk_node_ptr[b];
+  const int nl = p.blk_node_ptr[b + 1] - n0;
+  T* Xs = smem;
+  T* Us = Xs + nl * D;
+  T* Ws = Us + (C::NEED_U ? nl * V : 0);
+  T* Ys = Ws + (C::NEED_W ? nl * V : 0);
+
+  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+    const int64_t g = __ldg(p.lnode_gid + n0 + l);
+#pragma unroll
+    for (int d = 0; d < D; ++d) Xs[l * D + d] = coords[g * D + d];
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const int64_t dof = g * V + i;
+      if constexpr (C::NEED_U) Us[l * V + i] = u[dof];
+      if constexpr (C::NEED_W) Ws[l * V + i] = (fixed && fixed[dof]) ? T(0) : v[dof];
+      Ys[l * V + i] = T(0);
+    }
+  }
+  __syncthreads();
+
+  const int e_base = p.blk_elem_ptr[b];
+  const int c_begin = p.blk_color_ptr[b];
+  const int c_last = p.blk_color_ptr[b + 1] - 1;
+  for (int c = c_begin; c < c_last; ++c) {
+    const int e_end = e_base + p.color_ofs[c + 1];
+    for (int e = e_base + p.color_ofs[c] + threadIdx.x; e < e_end; e += blockDim.x) {
+      int lc[NPAD];
+      load_lconn<NPAD>(p.lconn + (int64_t)e * NPAD, lc);
+      T X[NN][D], U[NN][V], W[NN][V], Y[NN][V];
+#pragma unroll
+      for (int a = 0; a < NN; ++a) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) X[a][d] = Xs[lc[a] * D + d];
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          U[a][i] = C::NEED_U ? Us[lc[a] * V + i] : T(0);
+          W[a][i] = C::NEED_W ? Ws[lc[a] * V + i] : T(0);
+        }
+      }
+      const T k0 = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
+      element_apply<ET, MAT, T, MODE>(k0, p1, X, U, W, Y);
+#pragma unroll
+      for (int a = 0; a < NN; ++a)
+#pragma unroll
+        for (int i = 0; i < V; ++i) Ys[lc[a] * V + i] += Y[a][i];
+    }
+    __syncthreads();
+  }
+
+  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+    const int64_t g = __ldg(p.lnode_gid + n0 + l);
+    const int slot = __ldg(p.lnode_slot + n0 + l);
+    if (slot < 0) {
+#pragma unroll
+      for (int i = 0; i < V; ++i) {
+        const int64_t dof = g * V + i;
+        T val = Ys[l * V + i];
+        if (fixed && fixed[dof])
+          val = (MODE == TG_MODE_HVP) ? v[dof] : (MODE == TG_MODE_DIAG ? T(1) : T(0));
+        y[dof] = val;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < V; ++i) partials[(int64_t)slot * V + i] = Ys[l * V + i];
+    }
+  }
+}
+
+template <class T, int V, int MODE>
+__global__ void shared_reduce_kernel(const tg_block_plan p, const T* __restrict__ partials,
+                                     const T* __restrict__ v, const uint8_t* __restrict__ fixed,
+                                     T* __restrict__ y) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= p.n_shared) return;
+  const int64_t g = p.shared_node[s];
+  T acc[V];
+#pragma unroll
+  for (int i = 0; i < V; ++i) acc[i] = T(0);
+  const int k1 = p.shared_ptr[s + 1];
+  for (int k = p.shared_ptr[s]; k < k1; ++k) {
+    const int64_t slot = p.shared_slots[k];
+#pragma unroll
+    for (int i = 0; i < V; ++i) acc[i] += partials[slot * V + i];
+  }
+#pragma unroll
+  for (int i = 0; i < V; ++i) {
+    const int64_t dof = g * V + i;
+    T val = acc[i];
+    if (fixed && fixed[dof])
+      val = (MODE == TG_MODE_HVP) ? v[dof] : (MODE == TG_MODE_DIAG ? T(1) : T(0));
+    y[dof] = val;
+  }
+}
+
+// ------------------------------------------------------------------ energy per element
+template <int ET, int MAT, class T>
+__global__ void energy_kernel(const T* __restrict__ coords, const int32_t* __restrict__ conn,
+                              int64_t n_elems, const T* __restrict__ u, T p0, T p1,
+                              const T* __restrict__ eparam, T* __restrict__ out) {
+  using E = Elem<ET>;
+  constexpr int NN = E::NN, D = E::D, V = LawDims<MAT, D>::V;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  T X[NN][D], U[NN][V];
+#pragma unroll
+  for (int a = 0; a < NN; ++a) {
+    const int64_t n = __ldg(conn + e * NN + a);
+#pragma unroll
+    for (int d = 0; d < D; ++d) X[a][d] = coords[n * D + d];
+#pragma unroll
+    for (int i = 0; i < V; ++i) U[a][i] = u[n * V + i];
+  }
+  const Law<MAT, D, T> law(eparam ? eparam[e] : p0, p1);
+  T acc = T(0);
+#pragma unroll
+  for (int q = 0; q < E::Q; ++q) {
+    T G[NN][D];
+    const T wd = qp_geometry<ET, T>(q, X, G) * E::template w<T>(q);
+    T H[V][D];
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        T s = T(0);
+#pragma unroll
+        for (int a = 0; a < NN; ++a) s += G[a][d] * U[a][i];
+        H[i][d] = s;
+      }
+    T uq = T(0);
+#pragma unroll
+    for (int a = 0; a < NN; ++a) uq += E::template N<T>(q, a) * U[a][0];
+    acc += wd * law.energy(H, uq);
+  }
+  out[e] = acc;
+}
+
+// ------------------------------------------------------------------ host side
+template <int MAT, class F>
+int dispatch_mat_impl(F&& f) {
+  return f(IntC<MAT>{});
+}
+
+template <class F>
+int dispatch_mat(int kind, F&& f) {
+  switch (kind) {
+    case TG_POISSON: return f(IntC<TG_POISSON>{});
+    case TG_LINEAR_ELASTIC: return f(IntC<TG_LINEAR_ELASTIC>{});
+    case TG_NEO_HOOKEAN: return f(IntC<TG_NEO_HOOKEAN>{});
+    default: return set_error(TG_ERR_VALUE, "unknown material kind %d", kind);
+  }
+}
+
+template <class F>
+int dispatch_mode(int mode, F&& f) {
+  switch (mode) {
+    case TG_MODE_RESIDUAL: return f(IntC<TG_MODE_RESIDUAL>{});
+    case TG_MODE_HVP: return f(IntC<TG_MODE_HVP>{});
+    case TG_MODE_DIAG: return f(IntC<TG_MODE_DIAG>{});
+    default: return set_error(TG_ERR_VALUE, "unknown mode %d", mode);
+  }
+}
+
+inline int plan_check(const tg_block_plan* p, int elem) {
+  if (!p) return set_error(TG_ERR_VALUE, "plan must not be NULL");
+  if (p->n_blocks < 0 || p->n_elems < 0) return set_error(TG_ERR_VALUE, "corrupt plan");
+  const int npad = (elem == TG_HEX8) ? 8 : 4;
+  if (p->nodes_per_elem_padded != npad)
+    return set_error(TG_ERR_VALUE, "plan was built for another element type");
+  if (p->threads != 0 && p->threads != 64 && p->threads != 128 && p->threads != 256)
+    return set_error(TG_ERR_VALUE, "plan.threads must be 0, 64, 128 or 256");
+  if (p->max_local_nodes < 0 || p->max_local_nodes > 65535)
+    return set_error(TG_ERR_VALUE, "plan.max_local_nodes out of range");
+  return TG_OK;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" size_t tg_apply_workspace_bytes(int elem, int prec, int mat_kind,
+                                           const tg_block_plan* plan) {
+  if (!plan) return 0;
+  int V = 1;
+  const int D = (elem == TG_TRI3) ? 2 : 3;
+  if (mat_kind == TG_LINEAR_ELASTIC) V = D;
+  if (mat_kind == TG_NEO_HOOKEAN) V = 3;
+  const size_t sz = (prec == TG_F32) ? 4 : 8;
+  return (size_t)plan->n_partials * V * sz;
+}
+
+extern "C" int tg_apply(int elem, int prec, int mode, const tg_material* mat,
+                        const tg_block_plan* plan, const void* coords, int64_t n_nodes,
+                        const void* u, const void* v, const uint8_t* fixed, void* y,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  TG_TRY(plan_check(plan, elem));
+  TG_TRY(check_ptr(mat, "mat"));
+  TG_TRY(check_ptr(y, "y"));
+  if (n_nodes <= 0) return set_error(TG_ERR_VALUE, "n_nodes must be positive");
+  if (workspace_bytes < tg_apply_workspace_bytes(elem, prec, mat->kind, plan))
+    return set_error(TG_ERR_WORKSPACE, "tg_apply: workspace too small (%zu < %zu)",
+                     workspace_bytes, tg_apply_workspace_bytes(elem, prec, mat->kind, plan));
+  if (plan->n_blocks == 0) return TG_OK;
+  TG_TRY(check_ptr(coords, "coords"));
+  cudaStream_t st = as_stream(stream);
+  return dispatch_elem(elem, [&](auto et) -> int {
+    constexpr int ET = decltype(et)::value;
+    return dispatch_mat(mat->kind, [&](auto mk) -> int {
+      constexpr int MAT = decltype(mk)::value;
+      if constexpr (!Supported<ET, MAT>::value) {
+        return set_error(TG_ERR_UNSUPPORTED, "material %d is not available for element %d", MAT, ET);
+      } else {
+        return dispatch_prec(prec, [&](auto t) -> int {
+          using T = decltype(t);
+          return dispatch_mode(mode, [&](auto md) -> int {
+            constexpr int MODE = decltype(md)::value;
+            using C = ApplyCfg<ET, MAT, T, MODE>;
+            if (C::NEED_U && !u) return set_error(TG_ERR_VALUE, "u must not be NULL for this mode");
+            if (C::NEED_W && !v) return set_error(TG_ERR_VALUE, "v must not be NULL for HVP");
+            const size_t smem = (size_t)plan->max_local_nodes * C::WORDS_PER_NODE * sizeof(T);
+            auto kern = block_apply_kernel<ET, MAT, T, MODE>;
+            static size_t configured = 0;
+            if (smem > 48 * 1024 && smem > configured) {
+              TG_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)smem),
+                                "tg_apply: shared memory attribute"));
+              configured = smem;
+            }
+            const int threads = plan->threads ? plan->threads : 256;
+            kern<<<plan->n_blocks, threads, smem, st>>>(
+                *plan, (const T*)coords, (const T*)u, (const T*)v, fixed, (T*)y, (T*)workspace,
+                (T)mat->p0, (T)mat->p1, (const T*)mat->elem_param);
+            TG_TRY(launch_check("tg_apply: block kernel"));
+            if (plan->n_shared > 0) {
+              shared_reduce_kernel<T, C::V, MODE><<<grid_for(plan->n_shared, 256), 256, 0, st>>>(
+                  *plan, (const T*)workspace, (const T*)v, fixed, (T*)y);
+              TG_TRY(launch_check("tg_apply: shared reduce"));
+            }
+            return TG_OK;
+          });
+        });
+      }
+    });
+  });
+}
+
+extern "C" int tg_energy_per_element(int elem, int prec, const tg_material* mat,
+                                     const void* coords, int64_t n_nodes, const int32_t* conn,
+                                     int64_t n_elems, const void* u, void* out, void* stream) {
+  TG_TRY(check_ptr(mat, "mat"));
+  TG_TRY(check_sizes(n_elems, n_nodes, 1));
+  if (n_elems == 0) return TG_OK;
+  TG_TRY(check_ptr(coords, "coords"));
+  TG_TRY(check_ptr(conn, "conn"));
+  TG_TRY(check_ptr(u, "u"));
+  TG_TRY(check_ptr(out, "out"));
+  return dispatch_elem(elem, [&](auto et) -> int {
+    constexpr int ET = decltype(et)::value;
+    return dispatch_mat(mat->kind, [&](auto mk) -> int {
+      constexpr int MAT = decltype(mk)::value;
+      if constexpr (!Supported<ET, MAT>::value) {
+        return set_error(TG_ERR_UNSUPPORTED, "material %d is not available for element %d", MAT, ET);
+      } else {
+        return dispatch_prec(prec, [&](auto t) -> int {
+          using T = decltype(t);
+          energy_kernel<ET, MAT, T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
+              (const T*)coords, conn, n_elems, (const T*)u, (T)mat->p0, (T)mat->p1,
+              (const T*)mat->elem_param, (T*)out);
+          return launch_check("tg_energy_per_element");
+        });
+      }
+    });
+  });
+}

@@ -1,0 +1,648 @@
+// Sparse and vector kernels (K7, K8) and the device-resident solvers built on them.
+//
+// The reference has no solver: users compose jax.scipy.sparse.linalg.cg with the
+// matrix-free HVP (README.md:93).  Here:
+//   * CSR SpMV (layout of ColoredMatrix.to_csr, tatva/sparse/base.py:76-81)
+//   * deterministic FP64 dot products: a fixed partition into DOT_CHUNKS chunks and a
+//     fixed tree order, independent of the GPU and of the launch, so repeated solves
+//     are bitwise identical
+//   * Jacobi-preconditioned CG whose scalars never leave the device; `check_every`
+//     iterations are captured once in a CUDA graph and replayed between host
+//     convergence checks; every loop is bounded by max_iter
+//   * mixed precision: FP32 CG inner solves (FP32 HVP, FP64 dots), FP64 iterative
+//     refinement on the true residual b - A64 x.
+#include <cmath>
+#include <vector>
+
+#include "tg_common.cuh"
+#include "tg_dispatch.cuh"
+
+namespace tg {
+
+constexpr int DOT_CHUNKS = 1024;
+constexpr int DOT_THREADS = 256;
+constexpr int SCAL_RZ = 0, SCAL_PQ = 1, SCAL_ALPHA = 2, SCAL_BETA = 3, SCAL_RR = 4,
+              SCAL_FLAG = 6, SCAL_N = 8;
+
+// ------------------------------------------------------------------ reductions
+template <int K>
+__device__ __forceinline__ void block_reduce_store(double (&v)[K], double* __restrict__ out) {
+  __shared__ double sh[K][DOT_THREADS];
+#pragma unroll
+  for (int k = 0; k < K; ++k) sh[k][threadIdx.x] = v[k];
+  __syncthreads();
+  for (int s = DOT_THREADS / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = sh[k][0];
+  }
+}
+
+__device__ __forceinline__ void chunk_range(int64_t n, int64_t& i0, int64_t& i1) {
+  const int64_t chunk = (n + DOT_CHUNKS - 1) / DOT_CHUNKS;
+  i0 = (int64_t)blockIdx.x * chunk;
+  i1 = min(n, i0 + chunk);
+}
+
+template <class T>
+__global__ void __launch_bounds__(DOT_THREADS)
+    dot_partial_kernel(const T* __restrict__ x, const T* __restrict__ y, int64_t n,
+                       double* __restrict__ part) {
+  int64_t i0, i1;
+  chunk_range(n, i0, i1);
+  double v[1] = {0.0};
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) v[0] += (double)x[i] * (double)y[i];
+  block_reduce_store<1>(v, part + blockIdx.x);
+}
+
+// sums DOT_CHUNKS partials (stride K) into out[k]
+template <int K>
+__global__ void __launch_bounds__(DOT_THREADS)
+    dot_final_kernel(const double* __restrict__ part, double* __restrict__ out) {
+  double v[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = 0.0;
+  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS)
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] += part[b * K + k];
+  block_reduce_store<K>(v, out);
+}
+
+// ------------------------------------------------------------------ vector kernels
+template <class T>
+__global__ void axpby_kernel(int64_t n, double a, const T* __restrict__ x, double b,
+                             T* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (T)(a * (double)x[i] + b * (double)y[i]);
+}
+
+template <class Ti, class To>
+__global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (To)in[i];
+}
+
+// ------------------------------------------------------------------ CSR
+template <class T>
+__global__ void spmv_kernel(int64_t n_rows, const int32_t* __restrict__ indptr,
+                            const int32_t* __restrict__ indices, const T* __restrict__ data,
+                            const T* __restrict__ x, T* __restrict__ y) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= n_rows) return;
+  const int k0 = __ldg(indptr + row), k1 = __ldg(indptr + row + 1);
+  T acc = T(0);
+  for (int k = k0 + lane; k < k1; k += 32) acc += __ldg(data + k) * x[__ldg(indices + k)];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[row] = acc;
+}
+
+template <class T>
+__global__ void csr_diag_kernel(int64_t n_rows, const int32_t* __restrict__ indptr,
+                                const int32_t* __restrict__ indices, const T* __restrict__ data,
+                                T* __restrict__ diag) {
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n_rows) return;
+  T d = T(0);
+  for (int k = indptr[row]; k < indptr[row + 1]; ++k)
+    if (indices[k] == row) d = data[k];
+  diag[row] = d;
+}
+
+template <class T>
+__global__ void csr_dirichlet_kernel(int64_t n_rows, const int32_t* __restrict__ indptr,
+                                     const int32_t* __restrict__ indices,
+                                     const uint8_t* __restrict__ fixed, T* __restrict__ data) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= n_rows) return;
+  const bool rf = fixed[row] != 0;
+  for (int k = indptr[row] + lane; k < indptr[row + 1]; k += 32) {
+    const int c = indices[k];
+    if (rf) data[k] = (c == row) ? T(1) : T(0);
+    else if (fixed[c]) data[k] = T(0);
+  }
+}
+
+// ------------------------------------------------------------------ CG kernels
+// z = r / diag, p = z, partials of (r.z, r.r)
+template <class T>
+__global__ void __launch_bounds__(DOT_THREADS)
+    cg_init_kernel(int64_t n, const T* __restrict__ r, const T* __restrict__ diag,
+                   T* __restrict__ z, T* __restrict__ p, double* __restrict__ part) {
+  int64_t i0, i1;
+  chunk_range(n, i0, i1);
+  double v[2] = {0.0, 0.0};
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) {
+    const T ri = r[i];
+    const T zi = ri / diag[i];
+    z[i] = zi;
+    p[i] = zi;
+    v[0] += (double)ri * (double)zi;
+    v[1] += (double)ri * (double)ri;
+  }
+  block_reduce_store<2>(v, part + 2 * blockIdx.x);
+}
+
+// scal[RZ] = rz, scal[RR] = rr from the two-slot partials
+__global__ void cg_init_final_kernel(const double* __restrict__ part, double* __restrict__ scal) {
+  double v[2] = {0.0, 0.0};
+  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS) {
+    v[0] += part[2 * b];
+    v[1] += part[2 * b + 1];
+  }
+  __shared__ double out[2];
+  block_reduce_store<2>(v, out);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    scal[SCAL_RZ] = out[0];
+    scal[SCAL_RR] = out[1];
+    scal[SCAL_FLAG] = 0.0;
+  }
+}
+
+// alpha = rz / pq (breakdown flag on pq <= 0 or non-finite)
+__global__ void cg_alpha_kernel(const double* __restrict__ part, double* __restrict__ scal) {
+  double v[1] = {0.0};
+  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS) v[0] += part[b];
+  __shared__ double out[1];
+  block_reduce_store<1>(v, out);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double pq = out[0];
+    scal[SCAL_PQ] = pq;
+    const bool bad = !(pq > 0.0) || !isfinite(pq) || scal[SCAL_FLAG] != 0.0;
+    if (bad) scal[SCAL_FLAG] = 1.0;
+    scal[SCAL_ALPHA] = bad ? 0.0 : scal[SCAL_RZ] / pq;
+  }
+}
+
+// x += alpha p; r -= alpha q; z = r/diag; partials of (r.z, r.r)
+template <class T>
+__global__ void __launch_bounds__(DOT_THREADS)
+    cg_update_kernel(int64_t n, const double* __restrict__ scal, T* __restrict__ x,
+                     T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
+                     const T* __restrict__ q, const T* __restrict__ diag,
+                     double* __restrict__ part) {
+  int64_t i0, i1;
+  chunk_range(n, i0, i1);
+  const T alpha = (T)scal[SCAL_ALPHA];
+  double v[2] = {0.0, 0.0};
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) {
+    x[i] += alpha * p[i];
+    const T ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    const T zi = ri / diag[i];
+    z[i] = zi;
+    v[0] += (double)ri * (double)zi;
+    v[1] += (double)ri * (double)ri;
+  }
+  block_reduce_store<2>(v, part + 2 * blockIdx.x);
+}
+
+// beta = rz_new / rz; rz = rz_new; rr stored
+__global__ void cg_beta_kernel(const double* __restrict__ part, double* __restrict__ scal) {
+  double v[2] = {0.0, 0.0};
+  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS) {
+    v[0] += part[2 * b];
+    v[1] += part[2 * b + 1];
+  }
+  __shared__ double out[2];
+  block_reduce_store<2>(v, out);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double rz_new = out[0];
+    const bool bad = scal[SCAL_FLAG] != 0.0 || !isfinite(rz_new);
+    if (bad) scal[SCAL_FLAG] = 1.0;
+    scal[SCAL_BETA] = bad ? 0.0 : rz_new / scal[SCAL_RZ];
+    if (!bad) scal[SCAL_RZ] = rz_new;
+    scal[SCAL_RR] = out[1];
+  }
+}
+
+template <class T>
+__global__ void cg_p_kernel(int64_t n, const double* __restrict__ scal, const T* __restrict__ z,
+                            T* __restrict__ p) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = z[i] + (T)scal[SCAL_BETA] * p[i];
+}
+
+// out = (T)(r64 / s) with s = sqrt(rr) read on the device
+template <class T>
+__global__ void scale_down_kernel(int64_t n, const double* __restrict__ r64,
+                                  const double* __restrict__ s2, T* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)(r64[i] / sqrt(s2[0]));
+}
+template <class T>
+__global__ void scale_up_add_kernel(int64_t n, const T* __restrict__ d,
+                                    const double* __restrict__ s2, double* __restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] += sqrt(s2[0]) * (double)d[i];
+}
+
+// ------------------------------------------------------------------ operator description
+inline int op_values(const tg_operator_desc* op) {
+  const int D = (op->elem == TG_TRI3) ? 2 : 3;
+  if (op->mat.kind == TG_LINEAR_ELASTIC) return D;
+  if (op->mat.kind == TG_NEO_HOOKEAN) return 3;
+  return 1;
+}
+inline int64_t op_ndofs(const tg_operator_desc* op) {
+  return op->csr_data ? op->n_rows : op->n_nodes * op_values(op);
+}
+inline size_t prec_size(int prec) { return prec == TG_F32 ? 4 : 8; }
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Carve {
+  char* base;
+  size_t off = 0;
+  void* take(size_t bytes) {
+    void* p = base + off;
+    off += align256(bytes);
+    return p;
+  }
+};
+
+}  // namespace tg
+
+using namespace tg;
+
+// ============================================================================ C ABI
+extern "C" int tg_spmv(int prec, int64_t n_rows, const int32_t* indptr, const int32_t* indices,
+                       const void* data, const void* x, void* y, void* stream) {
+  if (n_rows < 0) return set_error(TG_ERR_VALUE, "negative size");
+  if (n_rows == 0) return TG_OK;
+  TG_TRY(check_ptr(indptr, "indptr"));
+  TG_TRY(check_ptr(indices, "indices"));
+  TG_TRY(check_ptr(data, "data"));
+  TG_TRY(check_ptr(x, "x"));
+  TG_TRY(check_ptr(y, "y"));
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    spmv_kernel<T><<<grid_for(n_rows * 32, 256), 256, 0, as_stream(stream)>>>(
+        n_rows, indptr, indices, (const T*)data, (const T*)x, (T*)y);
+    return launch_check("tg_spmv");
+  });
+}
+
+extern "C" int tg_csr_diagonal(int prec, int64_t n_rows, const int32_t* indptr,
+                               const int32_t* indices, const void* data, void* diag,
+                               void* stream) {
+  if (n_rows < 0) return set_error(TG_ERR_VALUE, "negative size");
+  if (n_rows == 0) return TG_OK;
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    csr_diag_kernel<T><<<grid_for(n_rows, 256), 256, 0, as_stream(stream)>>>(
+        n_rows, indptr, indices, (const T*)data, (T*)diag);
+    return launch_check("tg_csr_diagonal");
+  });
+}
+
+extern "C" int tg_csr_apply_dirichlet(int prec, int64_t n_rows, const int32_t* indptr,
+                                      const int32_t* indices, const uint8_t* fixed, void* data,
+                                      void* stream) {
+  if (n_rows < 0) return set_error(TG_ERR_VALUE, "negative size");
+  if (n_rows == 0 || fixed == nullptr) return TG_OK;
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    csr_dirichlet_kernel<T><<<grid_for(n_rows * 32, 256), 256, 0, as_stream(stream)>>>(
+        n_rows, indptr, indices, fixed, (T*)data);
+    return launch_check("tg_csr_apply_dirichlet");
+  });
+}
+
+extern "C" size_t tg_dot_workspace_bytes(void) { return (size_t)DOT_CHUNKS * 2 * sizeof(double); }
+
+extern "C" int tg_dot(int prec, const void* x, const void* y, int64_t n, double* out_dev,
+                      void* workspace, size_t workspace_bytes, void* stream) {
+  if (n < 0) return set_error(TG_ERR_VALUE, "negative size");
+  TG_TRY(check_ptr(out_dev, "out"));
+  if (workspace_bytes < tg_dot_workspace_bytes())
+    return set_error(TG_ERR_WORKSPACE, "tg_dot: workspace too small");
+  cudaStream_t st = as_stream(stream);
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>((const T*)x, (const T*)y, n,
+                                                              (double*)workspace);
+    dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>((const double*)workspace, out_dev);
+    return launch_check("tg_dot");
+  });
+}
+
+extern "C" int tg_axpby(int prec, int64_t n, double a, const void* x, double b, void* y,
+                        void* stream) {
+  if (n < 0) return set_error(TG_ERR_VALUE, "negative size");
+  if (n == 0) return TG_OK;
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    axpby_kernel<T><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(n, a, (const T*)x, b, (T*)y);
+    return launch_check("tg_axpby");
+  });
+}
+
+extern "C" int tg_convert(int prec_in, const void* in, int prec_out, void* out, int64_t n,
+                          void* stream) {
+  if (n < 0) return set_error(TG_ERR_VALUE, "negative size");
+  if (n == 0) return TG_OK;
+  return dispatch_prec(prec_in, [&](auto ti) -> int {
+    using Ti = decltype(ti);
+    return dispatch_prec(prec_out, [&](auto to) -> int {
+      using To = decltype(to);
+      convert_kernel<Ti, To><<<grid_for(n, 256), 256, 0, as_stream(stream)>>>((const Ti*)in,
+                                                                              (To*)out, n);
+      return launch_check("tg_convert");
+    });
+  });
+}
+
+extern "C" size_t tg_operator_workspace_bytes(const tg_operator_desc* op) {
+  if (!op || op->csr_data) return 0;
+  return tg_apply_workspace_bytes(op->elem, op->prec, op->mat.kind, op->plan);
+}
+
+extern "C" int tg_operator_apply(const tg_operator_desc* op, const void* x, void* y,
+                                 void* workspace, size_t workspace_bytes, void* stream) {
+  TG_TRY(check_ptr(op, "op"));
+  if (op->csr_data)
+    return tg_spmv(op->prec, op->n_rows, op->csr_indptr, op->csr_indices, op->csr_data, x, y,
+                   stream);
+  return tg_apply(op->elem, op->prec, TG_MODE_HVP, &op->mat, op->plan, op->coords, op->n_nodes,
+                  op->u, x, op->fixed, y, workspace, workspace_bytes, stream);
+}
+
+// ----------------------------------------------------------------------------- CG
+namespace tg {
+
+struct CgBuffers {
+  void *r, *z, *p, *q, *apply_ws;
+  double *part, *scal;
+  size_t apply_bytes;
+};
+
+static size_t cg_bytes(const tg_operator_desc* op) {
+  const int64_t n = op_ndofs(op);
+  const size_t vs = align256((size_t)n * prec_size(op->prec));
+  return 4 * vs + align256(tg_operator_workspace_bytes(op)) +
+         align256(DOT_CHUNKS * 2 * sizeof(double)) + align256(SCAL_N * sizeof(double));
+}
+
+static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
+  Carve c{(char*)ws};
+  const int64_t n = op_ndofs(op);
+  CgBuffers b;
+  const size_t vb = (size_t)n * prec_size(op->prec);
+  b.r = c.take(vb);
+  b.z = c.take(vb);
+  b.p = c.take(vb);
+  b.q = c.take(vb);
+  b.apply_bytes = tg_operator_workspace_bytes(op);
+  b.apply_ws = c.take(b.apply_bytes);
+  b.part = (double*)c.take(DOT_CHUNKS * 2 * sizeof(double));
+  b.scal = (double*)c.take(SCAL_N * sizeof(double));
+  return b;
+}
+
+// r = b - A x ; z = r/diag ; p = z ; scal <- (rz, rr)
+template <class T>
+static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* diag,
+                      CgBuffers& B, cudaStream_t st) {
+  const int64_t n = op_ndofs(op);
+  TG_TRY(tg_operator_apply(op, x, B.r, B.apply_ws, B.apply_bytes, st));
+  axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
+  cg_init_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(n, (const T*)B.r, diag, (T*)B.z,
+                                                        (T*)B.p, B.part);
+  cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal);
+  return launch_check("cg restart");
+}
+
+template <class T>
+static int cg_iteration(const tg_operator_desc* op, T* x, const T* diag, CgBuffers& B,
+                        cudaStream_t st) {
+  const int64_t n = op_ndofs(op);
+  TG_TRY(tg_operator_apply(op, B.p, B.q, B.apply_ws, B.apply_bytes, st));
+  dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n,
+                                                            B.part);
+  cg_alpha_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal);
+  cg_update_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(n, B.scal, x, (T*)B.r, (T*)B.z,
+                                                          (const T*)B.p, (const T*)B.q, diag,
+                                                          B.part);
+  cg_beta_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal);
+  cg_p_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, B.scal, (const T*)B.z, (T*)B.p);
+  return launch_check("cg iteration");
+}
+
+static int read_scalars(const double* dev, double* host, cudaStream_t st) {
+  TG_TRY(cuda_check(cudaMemcpyAsync(host, dev, SCAL_N * sizeof(double), cudaMemcpyDeviceToHost, st),
+                    "cg: read scalars"));
+  return cuda_check(cudaStreamSynchronize(st), "cg: synchronize");
+}
+
+// Runs CG from the current x until sqrt(rr) <= tol_abs (recursive residual) or the
+// iteration budget is spent.  Returns TG_OK, TG_ERR_NOT_CONVERGED or TG_ERR_BREAKDOWN.
+template <class T>
+static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag, double tol_abs,
+                  int max_iter, int check_every, CgBuffers& B, cudaStream_t st, int* iters) {
+  double h[SCAL_N];
+  TG_TRY(cg_restart<T>(op, bvec, x, diag, B, st));
+  TG_TRY(read_scalars(B.scal, h, st));
+  *iters = 0;
+  if (!std::isfinite(h[SCAL_RR])) return set_error(TG_ERR_BREAKDOWN, "cg: non-finite residual");
+  if (std::sqrt(h[SCAL_RR]) <= tol_abs) return TG_OK;
+  check_every = check_every < 1 ? 1 : check_every;
+  cudaGraphExec_t exec = nullptr;
+  int graph_len = 0;
+  const bool can_capture = (st != nullptr) && (st != cudaStreamLegacy) && (st != cudaStreamPerThread);
+  int rc = TG_OK;
+  while (*iters < max_iter) {
+    const int k = (max_iter - *iters) < check_every ? (max_iter - *iters) : check_every;
+    if (can_capture && k == check_every) {
+      if (!exec || graph_len != k) {
+        cudaGraph_t graph;
+        rc = cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cg: capture");
+        if (rc != TG_OK) break;
+        int rci = TG_OK;
+        for (int i = 0; i < k && rci == TG_OK; ++i) rci = cg_iteration<T>(op, x, diag, B, st);
+        cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (rci != TG_OK) { rc = rci; break; }
+        rc = cuda_check(ec, "cg: end capture");
+        if (rc != TG_OK) break;
+        if (exec) cudaGraphExecDestroy(exec);
+        rc = cuda_check(cudaGraphInstantiate(&exec, graph, 0), "cg: instantiate");
+        cudaGraphDestroy(graph);
+        if (rc != TG_OK) { exec = nullptr; break; }
+        graph_len = k;
+      }
+      rc = cuda_check(cudaGraphLaunch(exec, st), "cg: graph launch");
+      if (rc != TG_OK) break;
+    } else {
+      for (int i = 0; i < k && rc == TG_OK; ++i) rc = cg_iteration<T>(op, x, diag, B, st);
+      if (rc != TG_OK) break;
+    }
+    *iters += k;
+    rc = read_scalars(B.scal, h, st);
+    if (rc != TG_OK) break;
+    if (h[SCAL_FLAG] != 0.0 || !std::isfinite(h[SCAL_RR])) {
+      rc = set_error(TG_ERR_BREAKDOWN, "cg: breakdown (p.Ap <= 0 or non-finite) after %d iterations", *iters);
+      break;
+    }
+    if (std::sqrt(h[SCAL_RR]) <= tol_abs) break;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (rc != TG_OK) return rc;
+  if (std::sqrt(h[SCAL_RR]) > tol_abs)
+    return set_error(TG_ERR_NOT_CONVERGED, "cg: not converged in %d iterations", *iters);
+  return TG_OK;
+}
+
+template <class T>
+static int true_residual_norm(const tg_operator_desc* op, const T* bvec, const T* x,
+                              CgBuffers& B, cudaStream_t st, double* rn, double* bn) {
+  const int64_t n = op_ndofs(op);
+  TG_TRY(tg_operator_apply(op, x, B.r, B.apply_ws, B.apply_bytes, st));
+  axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
+  dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>((const T*)B.r, (const T*)B.r, n, B.part);
+  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(B.part, B.scal + 5);
+  dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(bvec, bvec, n, B.part);
+  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(B.part, B.scal + 7);
+  TG_TRY(launch_check("true residual"));
+  double h[SCAL_N];
+  TG_TRY(read_scalars(B.scal, h, st));
+  *rn = std::sqrt(h[5]);
+  *bn = std::sqrt(h[7]);
+  return TG_OK;
+}
+
+}  // namespace tg
+
+extern "C" size_t tg_cg_workspace_bytes(const tg_operator_desc* op) {
+  return op ? cg_bytes(op) : 0;
+}
+
+extern "C" int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, const void* diag,
+                           double rtol, int max_iter, int check_every, void* workspace,
+                           size_t workspace_bytes, tg_solve_stats* stats, void* stream) {
+  TG_TRY(check_ptr(op, "op"));
+  TG_TRY(check_ptr(b, "b"));
+  TG_TRY(check_ptr(x, "x"));
+  TG_TRY(check_ptr(diag, "diag"));
+  if (workspace_bytes < cg_bytes(op)) return set_error(TG_ERR_WORKSPACE, "tg_cg_solve: workspace too small");
+  if (!(rtol > 0.0) || max_iter < 0) return set_error(TG_ERR_VALUE, "bad rtol / max_iter");
+  cudaStream_t st = as_stream(stream);
+  CgBuffers B = cg_carve(op, workspace);
+  return dispatch_prec(op->prec, [&](auto t) -> int {
+    using T = decltype(t);
+    double rn = 0, bn = 0;
+    TG_TRY(true_residual_norm<T>(op, (const T*)b, (const T*)x, B, st, &rn, &bn));
+    int total = 0, rc = TG_OK;
+    const double tol = rtol * bn;
+    // restart on the true residual until it meets the tolerance (bounded by max_iter)
+    for (int restart = 0; restart < 8 && rn > tol && total < max_iter; ++restart) {
+      int it = 0;
+      rc = cg_run<T>(op, (const T*)b, (T*)x, (const T*)diag, 0.5 * tol, max_iter - total,
+                     check_every, B, st, &it);
+      total += it;
+      TG_TRY(true_residual_norm<T>(op, (const T*)b, (const T*)x, B, st, &rn, &bn));
+      if (rc != TG_OK) break;
+    }
+    if (stats) {
+      stats->iterations = total;
+      stats->outer = 0;
+      stats->rel_res = bn > 0 ? rn / bn : rn;
+    }
+    if (rc == TG_OK && rn > tol) rc = set_error(TG_ERR_NOT_CONVERGED, "tg_cg_solve: not converged");
+    if (stats) stats->status = rc;
+    return rc;
+  });
+}
+
+// ----------------------------------------------------------------------------- mixed
+extern "C" size_t tg_mixed_workspace_bytes(const tg_operator_desc* op64,
+                                           const tg_operator_desc* op32) {
+  if (!op64 || !op32) return 0;
+  const int64_t n = op_ndofs(op64);
+  return cg_bytes(op32) + align256(tg_operator_workspace_bytes(op64)) +
+         2 * align256((size_t)n * sizeof(double)) + 3 * align256((size_t)n * sizeof(float)) +
+         align256(DOT_CHUNKS * sizeof(double)) + align256(8 * sizeof(double));
+}
+
+extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_desc* op32,
+                              const double* b, double* x, const double* diag64, double rtol,
+                              double inner_rtol, int max_outer, int max_inner, int check_every,
+                              void* workspace, size_t workspace_bytes, tg_solve_stats* stats,
+                              void* stream) {
+  TG_TRY(check_ptr(op64, "op64"));
+  TG_TRY(check_ptr(op32, "op32"));
+  TG_TRY(check_ptr(b, "b"));
+  TG_TRY(check_ptr(x, "x"));
+  TG_TRY(check_ptr(diag64, "diag64"));
+  if (op64->prec != TG_F64 || op32->prec != TG_F32)
+    return set_error(TG_ERR_TYPE, "tg_mixed_solve: op64 must be FP64 and op32 FP32");
+  const int64_t n = op_ndofs(op64);
+  if (op_ndofs(op32) != n) return set_error(TG_ERR_VALUE, "tg_mixed_solve: operator sizes differ");
+  if (workspace_bytes < tg_mixed_workspace_bytes(op64, op32))
+    return set_error(TG_ERR_WORKSPACE, "tg_mixed_solve: workspace too small");
+  cudaStream_t st = as_stream(stream);
+  Carve c{(char*)workspace};
+  CgBuffers B = cg_carve(op32, c.take(cg_bytes(op32)));
+  const size_t ab64 = tg_operator_workspace_bytes(op64);
+  void* aws64 = c.take(ab64);
+  double* r64 = (double*)c.take(n * sizeof(double));
+  double* t64 = (double*)c.take(n * sizeof(double));
+  float* r32 = (float*)c.take(n * sizeof(float));
+  float* d32 = (float*)c.take(n * sizeof(float));
+  float* diag32 = (float*)c.take(n * sizeof(float));
+  double* part = (double*)c.take(DOT_CHUNKS * sizeof(double));
+  double* sc = (double*)c.take(8 * sizeof(double));
+
+  convert_kernel<double, float><<<grid_for(n, 256), 256, 0, st>>>(diag64, diag32, n);
+  // |b|^2
+  dot_partial_kernel<double><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(b, b, n, part);
+  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(part, sc + 1);
+  TG_TRY(launch_check("mixed: setup"));
+  int total_inner = 0, outer = 0, rc = TG_OK;
+  double rn = 0.0, bn = 0.0;
+  double h[8];
+  for (;;) {
+    // true residual r64 = b - A64 x in FP64
+    TG_TRY(tg_operator_apply(op64, x, r64, aws64, ab64, st));
+    axpby_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, b, -1.0, r64);
+    dot_partial_kernel<double><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(r64, r64, n, part);
+    dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(part, sc);
+    TG_TRY(launch_check("mixed: residual"));
+    TG_TRY(cuda_check(cudaMemcpyAsync(h, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, st), "mixed: read"));
+    TG_TRY(cuda_check(cudaStreamSynchronize(st), "mixed: sync"));
+    rn = std::sqrt(h[0]);
+    bn = std::sqrt(h[1]);
+    if (!std::isfinite(rn)) { rc = set_error(TG_ERR_BREAKDOWN, "mixed: non-finite residual"); break; }
+    if (rn <= rtol * bn || bn == 0.0) break;
+    if (outer >= max_outer) { rc = set_error(TG_ERR_NOT_CONVERGED, "mixed: not converged after %d refinements", outer); break; }
+    // inner FP32 solve A32 d = r64 / |r64|, d0 = 0
+    scale_down_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, r64, sc, r32);
+    TG_TRY(cuda_check(cudaMemsetAsync(d32, 0, n * sizeof(float), st), "mixed: zero"));
+    int it = 0;
+    const int irc = cg_run<float>(op32, r32, d32, diag32, inner_rtol, max_inner, check_every, B, st, &it);
+    total_inner += it;
+    if (irc == TG_ERR_BREAKDOWN) { rc = irc; break; }
+    if (irc != TG_OK && irc != TG_ERR_NOT_CONVERGED) { rc = irc; break; }
+    // x += |r64| d
+    scale_up_add_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, d32, sc, x);
+    TG_TRY(launch_check("mixed: update"));
+    ++outer;
+  }
+  (void)t64;
+  if (stats) {
+    stats->status = rc;
+    stats->iterations = total_inner;
+    stats->outer = outer;
+    stats->rel_res = bn > 0 ? rn / bn : rn;
+  }
+  return rc;
+}

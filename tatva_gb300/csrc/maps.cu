@@ -1,0 +1,461 @@
+// Operator maps: eval / grad / integration weights / integrate / deterministic sums /
+// gather and the reverse-mode transposes (K1-K3).
+//
+// Reference semantics (tatva/operator.py):
+//   eval                     :358-377  out[e,q,v]   = sum_a N_a(xi_q) u[conn[e,a], v]
+//   grad                     :379-397  out[e,q,v,d] = sum_a dN_a/dx_d u[conn[e,a], v]
+//   get_integration_weights  :172-192  out[e,q]     = detJ(e,q) * w_q
+//   _integrate_quad_array    :344-356  out[e,v]     = sum_q quad[e,q,v] w[e,q]
+//   integrate                :307-319  sum over elements
+#include "tg_common.cuh"
+#include "tg_dispatch.cuh"
+
+namespace tg {
+
+constexpr int TPB_T = 256;
+
+// ------------------------------------------------------------------ eval
+template <int ET, class T>
+__global__ void eval_kernel(const T* __restrict__ nodal, int V, const int32_t* __restrict__ conn,
+                            int64_t n_elems, T* __restrict__ out) {
+  using E = Elem<ET>;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t total = n_elems * E::Q * V;
+  if (tid >= total) return;
+  const int v = (int)(tid % V);
+  const int64_t eq = tid / V;
+  const int q = (int)(eq % E::Q);
+  const int64_t e = eq / E::Q;
+  T acc = T(0);
+#pragma unroll
+  for (int a = 0; a < E::NN; ++a) {
+    const int64_t n = __ldg(conn + e * E::NN + a);
+    acc += E::template N<T>(q, a) * nodal[n * V + v];
+  }
+  out[tid] = acc;
+}
+
+// ------------------------------------------------------------------ gather coords
+template <int ET, class T>
+__device__ __forceinline__ void gather_coords(const T* __restrict__ coords,
+                                              const int32_t* __restrict__ conn, int64_t e,
+                                              T (&X)[Elem<ET>::NN][Elem<ET>::D],
+                                              int (&nid)[Elem<ET>::NN]) {
+  using E = Elem<ET>;
+#pragma unroll
+  for (int a = 0; a < E::NN; ++a) {
+    nid[a] = __ldg(conn + e * E::NN + a);
+#pragma unroll
+    for (int d = 0; d < E::D; ++d) X[a][d] = coords[(int64_t)nid[a] * E::D + d];
+  }
+}
+
+// ------------------------------------------------------------------ grad
+template <int ET, class T>
+__global__ void grad_kernel(const T* __restrict__ nodal, const T* __restrict__ coords, int V,
+                            const int32_t* __restrict__ conn, int64_t n_elems,
+                            T* __restrict__ out) {
+  using E = Elem<ET>;
+  constexpr int NN = E::NN, D = E::D;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  T X[NN][D];
+  int nid[NN];
+  gather_coords<ET, T>(coords, conn, e, X, nid);
+#pragma unroll
+  for (int q = 0; q < E::Q; ++q) {
+    T G[NN][D];
+    qp_geometry<ET, T>(q, X, G);
+    T* o = out + ((e * E::Q + q) * V) * D;
+    for (int v = 0; v < V; ++v) {
+      T g[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) g[d] = T(0);
+#pragma unroll
+      for (int a = 0; a < NN; ++a) {
+        const T u = nodal[(int64_t)nid[a] * V + v];
+#pragma unroll
+        for (int d = 0; d < D; ++d) g[d] += G[a][d] * u;
+      }
+#pragma unroll
+      for (int d = 0; d < D; ++d) o[v * D + d] = g[d];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ weights
+template <int ET, class T>
+__global__ void weights_kernel(const T* __restrict__ coords, const int32_t* __restrict__ conn,
+                               int64_t n_elems, T* __restrict__ out) {
+  using E = Elem<ET>;
+  constexpr int NN = E::NN, D = E::D;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  T X[NN][D];
+  int nid[NN];
+  gather_coords<ET, T>(coords, conn, e, X, nid);
+#pragma unroll
+  for (int q = 0; q < E::Q; ++q) {
+    T G[NN][D];
+    const T det = qp_geometry<ET, T>(q, X, G);
+    out[e * E::Q + q] = det * E::template w<T>(q);
+  }
+}
+
+// ------------------------------------------------------------------ integrate quad array
+template <class T>
+__global__ void integrate_quad_kernel(const T* __restrict__ quad, const T* __restrict__ w,
+                                      int64_t n_elems, int Q, int V, T* __restrict__ out) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n_elems * V) return;
+  const int v = (int)(tid % V);
+  const int64_t e = tid / V;
+  T acc = T(0);
+  for (int q = 0; q < Q; ++q) acc += quad[(e * Q + q) * V + v] * w[e * Q + q];
+  out[tid] = acc;
+}
+
+// ------------------------------------------------------------------ deterministic row sums
+// Stage 1: a fixed number of chunks (independent of the GPU), each summed by one
+// block in a fixed strided + tree order, accumulated in FP64.  Stage 2: one block
+// sums the chunk partials in a fixed tree order.
+constexpr int SUM_CHUNKS = 512;
+constexpr int SUM_THREADS = 256;
+
+template <class T>
+__global__ void __launch_bounds__(SUM_THREADS)
+    rowsum_stage1(const T* __restrict__ in, int64_t n_rows, int V, double* __restrict__ part) {
+  __shared__ double sh[SUM_THREADS];
+  const int64_t chunk = (n_rows + SUM_CHUNKS - 1) / SUM_CHUNKS;
+  const int64_t r0 = blockIdx.x * chunk;
+  const int64_t r1 = min(n_rows, r0 + chunk);
+  for (int v = 0; v < V; ++v) {
+    double acc = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += SUM_THREADS) acc += (double)in[r * V + v];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = SUM_THREADS / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x * V + v] = sh[0];
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(SUM_THREADS)
+    rowsum_stage2(const double* __restrict__ part, int V, T* __restrict__ out) {
+  __shared__ double sh[SUM_THREADS];
+  for (int v = 0; v < V; ++v) {
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < SUM_CHUNKS; b += SUM_THREADS) acc += part[b * V + v];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = SUM_THREADS / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[v] = (T)sh[0];
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ gather
+template <class T>
+__global__ void gather_nodal_kernel(const T* __restrict__ nodal, int V,
+                                    const int32_t* __restrict__ conn, int64_t n_entries,
+                                    T* __restrict__ out) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n_entries * V) return;
+  const int v = (int)(tid % V);
+  const int64_t k = tid / V;
+  out[tid] = nodal[(int64_t)__ldg(conn + k) * V + v];
+}
+
+// ------------------------------------------------------------------ transposes
+template <int ET, class T>
+__global__ void grad_transpose_kernel(const T* __restrict__ flux, const T* __restrict__ coords,
+                                      int64_t n_nodes, int V, const int32_t* __restrict__ conn,
+                                      const int32_t* __restrict__ inc_ptr,
+                                      const int32_t* __restrict__ inc_idx, T* __restrict__ out) {
+  using E = Elem<ET>;
+  constexpr int NN = E::NN, D = E::D;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  for (int v = 0; v < V; ++v) out[n * V + v] = T(0);
+  for (int k = inc_ptr[n]; k < inc_ptr[n + 1]; ++k) {
+    const int ea = inc_idx[k];
+    const int64_t e = ea / NN;
+    const int a = ea % NN;
+    T X[NN][D];
+    int nid[NN];
+    gather_coords<ET, T>(coords, conn, e, X, nid);
+#pragma unroll
+    for (int q = 0; q < E::Q; ++q) {
+      T G[NN][D];
+      qp_geometry<ET, T>(q, X, G);
+      T ga[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        ga[d] = G[0][d];
+#pragma unroll
+        for (int b = 1; b < NN; ++b)
+          if (b == a) ga[d] = G[b][d];
+      }
+      const T* f = flux + ((e * E::Q + q) * V) * D;
+      for (int v = 0; v < V; ++v) {
+        T s = T(0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) s += ga[d] * f[v * D + d];
+        out[n * V + v] += s;
+      }
+    }
+  }
+}
+
+template <int ET, class T>
+__global__ void eval_transpose_kernel(const T* __restrict__ quad, int64_t n_nodes, int V,
+                                      const int32_t* __restrict__ inc_ptr,
+                                      const int32_t* __restrict__ inc_idx, T* __restrict__ out) {
+  using E = Elem<ET>;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  for (int v = 0; v < V; ++v) {
+    T acc = T(0);
+    for (int k = inc_ptr[n]; k < inc_ptr[n + 1]; ++k) {
+      const int ea = inc_idx[k];
+      const int64_t e = ea / E::NN;
+      const int a = ea % E::NN;
+      for (int q = 0; q < E::Q; ++q) acc += E::template N<T>(q, a) * quad[(e * E::Q + q) * V + v];
+    }
+    out[n * V + v] = acc;
+  }
+}
+
+template <class T>
+__global__ void integrate_quad_transpose_kernel(const T* __restrict__ g, const T* __restrict__ w,
+                                                int64_t n_elems, int Q, int V,
+                                                T* __restrict__ out) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n_elems * Q * V) return;
+  const int v = (int)(tid % V);
+  const int64_t eq = tid / V;
+  const int64_t e = eq / Q;
+  out[tid] = g[e * V + v] * w[eq];
+}
+
+template <class T>
+__global__ void scatter_nodal_kernel(const T* __restrict__ vals, int64_t n_nodes, int V,
+                                     const int32_t* __restrict__ inc_ptr,
+                                     const int32_t* __restrict__ inc_idx, T* __restrict__ out) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n_nodes * V) return;
+  const int v = (int)(tid % V);
+  const int64_t n = tid / V;
+  T acc = T(0);
+  for (int k = inc_ptr[n]; k < inc_ptr[n + 1]; ++k) acc += vals[(int64_t)inc_idx[k] * V + v];
+  out[tid] = acc;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" int tg_integrate_quad_transpose(int prec, const void* g, const void* weights,
+                                           int64_t n_elems, int n_quad, int n_vals, void* out,
+                                           void* stream) {
+  TG_TRY(check_sizes(n_elems, 0, n_vals));
+  if (n_quad <= 0) return set_error(TG_ERR_VALUE, "n_quad must be positive");
+  if (n_elems == 0) return TG_OK;
+  TG_TRY(check_ptr(g, "g"));
+  TG_TRY(check_ptr(weights, "weights"));
+  TG_TRY(check_ptr(out, "out"));
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    const int64_t total = n_elems * n_quad * n_vals;
+    integrate_quad_transpose_kernel<T><<<grid_for(total, TPB_T), TPB_T, 0, as_stream(stream)>>>(
+        (const T*)g, (const T*)weights, n_elems, n_quad, n_vals, (T*)out);
+    return launch_check("tg_integrate_quad_transpose");
+  });
+}
+
+extern "C" int tg_scatter_nodal(int prec, const void* vals, int64_t n_nodes, int n_vals,
+                                int nodes_per_elem, const int32_t* inc_ptr,
+                                const int32_t* inc_idx, void* out, void* stream) {
+  (void)nodes_per_elem;
+  TG_TRY(check_sizes(0, n_nodes, n_vals));
+  if (n_nodes == 0) return TG_OK;
+  TG_TRY(check_ptr(inc_ptr, "inc_ptr"));
+  TG_TRY(check_ptr(out, "out"));
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    scatter_nodal_kernel<T><<<grid_for(n_nodes * n_vals, TPB_T), TPB_T, 0, as_stream(stream)>>>(
+        (const T*)vals, n_nodes, n_vals, inc_ptr, inc_idx, (T*)out);
+    return launch_check("tg_scatter_nodal");
+  });
+}
+
+static constexpr int TPB = 256;
+
+extern "C" int tg_eval(int elem, int prec, const void* nodal, int64_t n_nodes, int n_vals,
+                       const int32_t* conn, int64_t n_elems, void* out, void* stream) {
+  TG_TRY(check_sizes(n_elems, n_nodes, n_vals));
+  if (n_elems == 0) return TG_OK;
+  TG_TRY(check_ptr(nodal, "nodal"));
+  TG_TRY(check_ptr(conn, "conn"));
+  TG_TRY(check_ptr(out, "out"));
+  return dispatch_elem(elem, [&](auto et) -> int {
+    constexpr int ET = decltype(et)::value;
+    return dispatch_prec(prec, [&](auto t) -> int {
+      using T = decltype(t);
+      const int64_t total = n_elems * Elem<ET>::Q * n_vals;
+      eval_kernel<ET, T><<<grid_for(total, TPB), TPB, 0, as_stream(stream)>>>(
+          (const T*)nodal, n_vals, conn, n_elems, (T*)out);
+      return launch_check("tg_eval");
+    });
+  });
+}
+
+extern "C" int tg_grad(int elem, int prec, const void* nodal, const void* coords, int64_t n_nodes,
+                       int n_vals, const int32_t* conn, int64_t n_elems, void* out, void* stream) {
+  TG_TRY(check_sizes(n_elems, n_nodes, n_vals));
+  if (n_elems == 0) return TG_OK;
+  TG_TRY(check_ptr(nodal, "nodal"));
+  TG_TRY(check_ptr(coords, "coords"));
+  TG_TRY(check_ptr(conn, "conn"));
+  TG_TRY(check_ptr(out, "out"));
+  return dispatch_elem(elem, [&](auto et) -> int {
+    constexpr int ET = decltype(et)::value;
+    return dispatch_prec(prec, [&](auto t) -> int {
+      using T = decltype(t);
+      grad_kernel<ET, T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
+          (const T*)nodal, (const T*)coords, n_vals, conn, n_elems, (T*)out);
+      return launch_check("tg_grad");
+    });
+  });
+}
+
+extern "C" int tg_integration_weights(int elem, int prec, const void* coords, int64_t n_nodes,
+                                      const int32_t* conn, int64_t n_elems, void* out,
+                                      void* stream) {
+  TG_TRY(check_sizes(n_elems, n_nodes, 1));
+  if (n_elems == 0) return TG_OK;
+  TG_TRY(check_ptr(coords, "coords"));
+  TG_TRY(check_ptr(conn, "conn"));
+  TG_TRY(check_ptr(out, "out"));
+  return dispatch_elem(elem, [&](auto et) -> int {
+    constexpr int ET = decltype(et)::value;
+    return dispatch_prec(prec, [&](auto t) -> int {
+      using T = decltype(t);
+      weights_kernel<ET, T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
+          (const T*)coords, conn, n_elems, (T*)out);
+      return launch_check("tg_integration_weights");
+    });
+  });
+}
+
+extern "C" int tg_integrate_quad(int prec, const void* quad, const void* weights, int64_t n_elems,
+                                 int n_quad, int n_vals, void* out, void* stream) {
+  TG_TRY(check_sizes(n_elems, 0, n_vals));
+  if (n_quad <= 0) return set_error(TG_ERR_VALUE, "n_quad must be positive");
+  if (n_elems == 0) return TG_OK;
+  TG_TRY(check_ptr(quad, "quad"));
+  TG_TRY(check_ptr(weights, "weights"));
+  TG_TRY(check_ptr(out, "out"));
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    integrate_quad_kernel<T><<<grid_for(n_elems * n_vals, TPB), TPB, 0, as_stream(stream)>>>(
+        (const T*)quad, (const T*)weights, n_elems, n_quad, n_vals, (T*)out);
+    return launch_check("tg_integrate_quad");
+  });
+}
+
+extern "C" size_t tg_sum_rows_workspace_bytes(int prec, int n_vals) {
+  (void)prec;
+  return (size_t)SUM_CHUNKS * (size_t)(n_vals > 0 ? n_vals : 1) * sizeof(double);
+}
+
+extern "C" int tg_sum_rows(int prec, const void* in, int64_t n_rows, int n_vals, void* out,
+                           void* workspace, size_t workspace_bytes, void* stream) {
+  if (n_rows < 0 || n_vals <= 0) return set_error(TG_ERR_VALUE, "bad sizes for tg_sum_rows");
+  TG_TRY(check_ptr(out, "out"));
+  if (workspace_bytes < tg_sum_rows_workspace_bytes(prec, n_vals))
+    return set_error(TG_ERR_WORKSPACE, "tg_sum_rows: workspace too small");
+  if (n_rows > 0) TG_TRY(check_ptr(in, "in"));
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    rowsum_stage1<T><<<SUM_CHUNKS, SUM_THREADS, 0, as_stream(stream)>>>(
+        (const T*)in, n_rows, n_vals, (double*)workspace);
+    rowsum_stage2<T><<<1, SUM_THREADS, 0, as_stream(stream)>>>((const double*)workspace, n_vals,
+                                                               (T*)out);
+    return launch_check("tg_sum_rows");
+  });
+}
+
+extern "C" int tg_gather_nodal(int prec, const void* nodal, int64_t n_nodes, int n_vals,
+                               const int32_t* conn, int64_t n_elems, int nodes_per_elem,
+                               void* out, void* stream) {
+  TG_TRY(check_sizes(n_elems, n_nodes, n_vals));
+  if (nodes_per_elem <= 0) return set_error(TG_ERR_VALUE, "nodes_per_elem must be positive");
+  if (n_elems == 0) return TG_OK;
+  TG_TRY(check_ptr(nodal, "nodal"));
+  TG_TRY(check_ptr(conn, "conn"));
+  TG_TRY(check_ptr(out, "out"));
+  const int64_t entries = n_elems * nodes_per_elem;
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    gather_nodal_kernel<T><<<grid_for(entries * n_vals, TPB), TPB, 0, as_stream(stream)>>>(
+        (const T*)nodal, n_vals, conn, entries, (T*)out);
+    return launch_check("tg_gather_nodal");
+  });
+}
+
+extern "C" int tg_grad_transpose(int elem, int prec, const void* flux, const void* coords,
+                                 int64_t n_nodes, int n_vals, const int32_t* conn,
+                                 int64_t n_elems, const int32_t* inc_ptr, const int32_t* inc_idx,
+                                 void* out, void* stream) {
+  TG_TRY(check_sizes(n_elems, n_nodes, n_vals));
+  if (n_nodes == 0) return TG_OK;
+  TG_TRY(check_ptr(coords, "coords"));
+  TG_TRY(check_ptr(inc_ptr, "inc_ptr"));
+  TG_TRY(check_ptr(out, "out"));
+  if (n_elems > 0) {
+    TG_TRY(check_ptr(flux, "flux"));
+    TG_TRY(check_ptr(conn, "conn"));
+    TG_TRY(check_ptr(inc_idx, "inc_idx"));
+  }
+  return dispatch_elem(elem, [&](auto et) -> int {
+    constexpr int ET = decltype(et)::value;
+    return dispatch_prec(prec, [&](auto t) -> int {
+      using T = decltype(t);
+      grad_transpose_kernel<ET, T><<<grid_for(n_nodes, 128), 128, 0, as_stream(stream)>>>(
+          (const T*)flux, (const T*)coords, n_nodes, n_vals, conn, inc_ptr, inc_idx, (T*)out);
+      return launch_check("tg_grad_transpose");
+    });
+  });
+}
+
+extern "C" int tg_eval_transpose(int elem, int prec, const void* quad, int64_t n_nodes,
+                                 int n_vals, const int32_t* conn, int64_t n_elems,
+                                 const int32_t* inc_ptr, const int32_t* inc_idx, void* out,
+                                 void* stream) {
+  (void)conn;
+  TG_TRY(check_sizes(n_elems, n_nodes, n_vals));
+  if (n_nodes == 0) return TG_OK;
+  TG_TRY(check_ptr(inc_ptr, "inc_ptr"));
+  TG_TRY(check_ptr(out, "out"));
+  if (n_elems > 0) {
+    TG_TRY(check_ptr(quad, "quad"));
+    TG_TRY(check_ptr(inc_idx, "inc_idx"));
+  }
+  return dispatch_elem(elem, [&](auto et) -> int {
+    constexpr int ET = decltype(et)::value;
+    return dispatch_prec(prec, [&](auto t) -> int {
+      using T = decltype(t);
+      eval_transpose_kernel<ET, T><<<grid_for(n_nodes, 128), 128, 0, as_stream(stream)>>>(
+          (const T*)quad, n_nodes, n_vals, inc_ptr, inc_idx, (T*)out);
+      return launch_check("tg_eval_transpose");
+    });
+  });
+}

@@ -1,0 +1,591 @@
+// Host-side setup (H1): sparsity pattern, distance-2 colouring, element colouring,
+// node incidence and the element-block plan used by the assembly kernels.
+//
+// Reference: tatva/sparse/_extraction.py _create_sparse_structure (:37-87) and
+// pattern_from_mesh (:90-102); tatva/sparse/_coloring.py get_distance2_adjacency
+// (:27-48), greedy_coloring (:136-153), distance2_colors (:270-283).  The reference
+// pins tatva_coloring.distance2_colors (external, tatva/sparse/base.py:32,66); the
+// in-repo natural-order greedy restated here is the one this project reproduces
+// bit for bit.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+#include "tatva_gb300.h"
+
+namespace tg {
+int set_error(int code, const char* fmt, ...);
+}
+using tg::set_error;
+
+namespace {
+
+template <class F>
+void parallel_for(int64_t n, F&& f) {
+  unsigned hc = std::thread::hardware_concurrency();
+  int nt = (int)(hc == 0 ? 1 : (hc > 32 ? 32 : hc));
+  if (n < 8192 || nt <= 1) {
+    f(0, n, 0);
+    return;
+  }
+  const int64_t chunk = (n + nt - 1) / nt;
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t) {
+    const int64_t a = t * chunk, b = std::min<int64_t>(n, a + chunk);
+    if (a >= b) break;
+    th.emplace_back([&, a, b, t] { f(a, b, t); });
+  }
+  for (auto& x : th) x.join();
+}
+
+int nthreads() {
+  unsigned hc = std::thread::hardware_concurrency();
+  return (int)(hc == 0 ? 1 : (hc > 32 ? 32 : hc));
+}
+
+int check_conn(const int32_t* conn, int64_t n_elems, int npe, int64_t n_nodes) {
+  if (!conn && n_elems > 0) return set_error(TG_ERR_VALUE, "conn must not be NULL");
+  if (n_elems < 0 || n_nodes < 0 || npe <= 0) return set_error(TG_ERR_VALUE, "bad mesh sizes");
+  if (n_nodes > INT32_MAX || n_elems * npe > INT32_MAX)
+    return set_error(TG_ERR_VALUE, "mesh too large for int32 indexing");
+  for (int64_t k = 0; k < n_elems * npe; ++k) {
+    if (conn[k] < 0) return set_error(TG_ERR_VALUE, "Mesh element connectivity contains negative node indices.");
+    if (conn[k] >= n_nodes)
+      return set_error(TG_ERR_VALUE,
+                       "Mesh element connectivity references nodes outside the mesh coordinates array.");
+  }
+  return TG_OK;
+}
+
+// node -> incident (e*npe + a), ascending e
+void incidence(const int32_t* conn, int64_t n_elems, int npe, int64_t n_nodes,
+               std::vector<int32_t>& ptr, std::vector<int32_t>& idx) {
+  ptr.assign(n_nodes + 1, 0);
+  for (int64_t k = 0; k < n_elems * npe; ++k) ptr[conn[k] + 1]++;
+  for (int64_t i = 0; i < n_nodes; ++i) ptr[i + 1] += ptr[i];
+  idx.resize(n_elems * npe);
+  std::vector<int32_t> pos(ptr.begin(), ptr.end() - 1);
+  for (int64_t k = 0; k < n_elems * npe; ++k) idx[pos[conn[k]]++] = (int32_t)k;
+}
+
+struct Pattern {
+  int64_t n_rows = 0;
+  std::vector<int32_t> indptr;
+  std::vector<int32_t> indices;
+};
+
+struct Plan {
+  int32_t n_blocks = 0, n_elems = 0, npad = 4, max_local = 0, max_colors = 0;
+  std::vector<int32_t> blk_elem_ptr, blk_color_ptr, color_ofs, blk_node_ptr, elem_id, lnode_gid,
+      lnode_slot, shared_node, shared_ptr, shared_slots;
+  std::vector<uint16_t> lconn;
+};
+
+uint64_t spread3(uint64_t x) {  // 21 bits -> every third bit
+  x &= 0x1fffff;
+  x = (x | x << 32) & 0x1f00000000ffffULL;
+  x = (x | x << 16) & 0x1f0000ff0000ffULL;
+  x = (x | x << 8) & 0x100f00f00f00f00fULL;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
+  x = (x | x << 2) & 0x1249249249249249ULL;
+  return x;
+}
+uint64_t spread2(uint64_t x) {  // 31 bits -> every second bit
+  x &= 0x7fffffff;
+  x = (x | x << 16) & 0x0000ffff0000ffffULL;
+  x = (x | x << 8) & 0x00ff00ff00ff00ffULL;
+  x = (x | x << 4) & 0x0f0f0f0f0f0f0f0fULL;
+  x = (x | x << 2) & 0x3333333333333333ULL;
+  x = (x | x << 1) & 0x5555555555555555ULL;
+  return x;
+}
+
+}  // namespace
+
+// ============================================================================ pattern
+extern "C" int tg_pattern_build(const int32_t* conn, int64_t n_elems, int npe, int64_t n_nodes,
+                                int ndpn, void** handle) {
+  if (!handle) return set_error(TG_ERR_VALUE, "handle must not be NULL");
+  *handle = nullptr;
+  if (ndpn <= 0) return set_error(TG_ERR_VALUE, "n_dofs_per_node must be positive");
+  int rc = check_conn(conn, n_elems, npe, n_nodes);
+  if (rc) return rc;
+  try {
+    std::vector<int32_t> iptr, iidx;
+    incidence(conn, n_elems, npe, n_nodes, iptr, iidx);
+    // node adjacency (sorted, unique, includes the node itself)
+    std::vector<int64_t> cnt(n_nodes + 1, 0);
+    const int nt = nthreads();
+    std::vector<std::vector<int32_t>> marks(nt);
+    parallel_for(n_nodes, [&](int64_t a, int64_t b, int t) {
+      auto& mark = marks[t];
+      mark.assign(n_nodes, -1);
+      for (int64_t p = a; p < b; ++p) {
+        int64_t c = 0;
+        for (int k = iptr[p]; k < iptr[p + 1]; ++k) {
+          const int64_t e = iidx[k] / npe;
+          for (int j = 0; j < npe; ++j) {
+            const int32_t q = conn[e * npe + j];
+            if (mark[q] != (int32_t)p) { mark[q] = (int32_t)p; ++c; }
+          }
+        }
+        cnt[p + 1] = c;
+      }
+    });
+    std::vector<int64_t> nptr(n_nodes + 1, 0);
+    for (int64_t p = 0; p < n_nodes; ++p) nptr[p + 1] = nptr[p] + cnt[p + 1];
+    std::vector<int32_t> nadj(nptr[n_nodes]);
+    parallel_for(n_nodes, [&](int64_t a, int64_t b, int t) {
+      auto& mark = marks[t];
+      std::fill(mark.begin(), mark.end(), -1);
+      for (int64_t p = a; p < b; ++p) {
+        int64_t o = nptr[p];
+        for (int k = iptr[p]; k < iptr[p + 1]; ++k) {
+          const int64_t e = iidx[k] / npe;
+          for (int j = 0; j < npe; ++j) {
+            const int32_t q = conn[e * npe + j];
+            if (mark[q] != (int32_t)p) { mark[q] = (int32_t)p; nadj[o++] = q; }
+          }
+        }
+        std::sort(nadj.begin() + nptr[p], nadj.begin() + nptr[p + 1]);
+      }
+    });
+    marks.clear();
+    const int64_t n_rows = n_nodes * ndpn;
+    int64_t nnz = 0;
+    for (int64_t p = 0; p < n_nodes; ++p) nnz += (nptr[p + 1] - nptr[p]) * ndpn * ndpn;
+    if (nnz > INT32_MAX || n_rows > INT32_MAX)
+      return set_error(TG_ERR_VALUE, "pattern has more than 2^31-1 entries");
+    auto* P = new Pattern();
+    P->n_rows = n_rows;
+    P->indptr.resize(n_rows + 1);
+    P->indices.resize(nnz);
+    P->indptr[0] = 0;
+    for (int64_t p = 0; p < n_nodes; ++p) {
+      const int32_t len = (int32_t)((nptr[p + 1] - nptr[p]) * ndpn);
+      for (int c = 0; c < ndpn; ++c) P->indptr[p * ndpn + c + 1] = P->indptr[p * ndpn + c] + len;
+    }
+    parallel_for(n_nodes, [&](int64_t a, int64_t b, int) {
+      for (int64_t p = a; p < b; ++p)
+        for (int c = 0; c < ndpn; ++c) {
+          int64_t o = P->indptr[p * ndpn + c];
+          for (int64_t k = nptr[p]; k < nptr[p + 1]; ++k)
+            for (int d = 0; d < ndpn; ++d) P->indices[o++] = (int32_t)((int64_t)nadj[k] * ndpn + d);
+        }
+    });
+    *handle = P;
+  } catch (const std::bad_alloc&) {
+    return set_error(TG_ERR_VALUE, "tg_pattern_build: out of host memory");
+  }
+  return TG_OK;
+}
+
+extern "C" int tg_pattern_nnz(const void* handle, int64_t* nnz) {
+  if (!handle || !nnz) return set_error(TG_ERR_VALUE, "NULL argument");
+  *nnz = (int64_t)static_cast<const Pattern*>(handle)->indices.size();
+  return TG_OK;
+}
+
+extern "C" int tg_pattern_export(const void* handle, int32_t* indptr, int32_t* indices) {
+  if (!handle) return set_error(TG_ERR_VALUE, "NULL handle");
+  const Pattern* P = static_cast<const Pattern*>(handle);
+  if (indptr) std::memcpy(indptr, P->indptr.data(), P->indptr.size() * sizeof(int32_t));
+  if (indices) std::memcpy(indices, P->indices.data(), P->indices.size() * sizeof(int32_t));
+  return TG_OK;
+}
+
+extern "C" void tg_pattern_free(void* handle) { delete static_cast<Pattern*>(handle); }
+
+// ============================================================================ colouring
+// Natural-order greedy over A @ A neighbourhoods.  Rows with identical column lists
+// ("groups", e.g. the ndpn dofs of one node) share their distance-2 neighbourhood;
+// each neighbourhood is scanned once per group and the group's rows are then
+// coloured in order, adding a freshly used colour to the forbidden set exactly when
+// that row lies in the neighbourhood -- the same result as scanning row by row.
+extern "C" int tg_distance2_colors(const int32_t* indptr, const int32_t* indices, int64_t n,
+                                   int32_t* colors, int32_t* n_colors) {
+  if (n < 0) return set_error(TG_ERR_VALUE, "negative size");
+  if (n == 0) {
+    if (n_colors) *n_colors = 0;
+    return TG_OK;
+  }
+  if (!indptr || !indices || !colors) return set_error(TG_ERR_VALUE, "NULL argument");
+  for (int64_t i = 0; i < n; ++i)
+    if (indptr[i + 1] < indptr[i]) return set_error(TG_ERR_VALUE, "indptr is not monotone");
+  const int64_t nnz = indptr[n];
+  for (int64_t k = 0; k < nnz; ++k)
+    if (indices[k] < 0 || indices[k] >= n) return set_error(TG_ERR_VALUE, "column index out of range");
+  try {
+    std::vector<int32_t> group_of(n), group_rep;
+    group_rep.reserve(n / 2 + 1);
+    for (int64_t i = 0; i < n; ++i) {
+      bool same = false;
+      if (i > 0) {
+        const int32_t l0 = indptr[i] - indptr[i - 1], l1 = indptr[i + 1] - indptr[i];
+        same = (l0 == l1) && std::memcmp(indices + indptr[i - 1], indices + indptr[i],
+                                         sizeof(int32_t) * l1) == 0;
+      }
+      if (!same) group_rep.push_back((int32_t)i);
+      group_of[i] = (int32_t)group_rep.size() - 1;
+    }
+    const int64_t ng = (int64_t)group_rep.size();
+    std::vector<int32_t> gseen(ng, -1), visited(n, -1), used;
+    used.reserve(256);
+    for (int64_t i = 0; i < n; ++i) colors[i] = -1;
+    int32_t maxc = -1;
+    for (int64_t g = 0; g < ng; ++g) {
+      const int32_t stamp = (int32_t)g;
+      const int32_t r0 = group_rep[g];
+      const int32_t r1 = (g + 1 < ng) ? group_rep[g + 1] : (int32_t)n;
+      for (int32_t k = indptr[r0]; k < indptr[r0 + 1]; ++k) {
+        const int32_t j = indices[k];
+        const int32_t gj = group_of[j];
+        if (gseen[gj] == stamp) continue;
+        gseen[gj] = stamp;
+        const int32_t rep = group_rep[gj];
+        for (int32_t kk = indptr[rep]; kk < indptr[rep + 1]; ++kk) {
+          const int32_t m = indices[kk];
+          if (visited[m] == stamp) continue;
+          visited[m] = stamp;
+          const int32_t cm = colors[m];
+          if (cm >= 0) {
+            if ((size_t)cm >= used.size()) used.resize(cm + 1, -1);
+            used[cm] = stamp;
+          }
+        }
+      }
+      for (int32_t r = r0; r < r1; ++r) {
+        int32_t c = 0;
+        while ((size_t)c < used.size() && used[c] == stamp) ++c;
+        colors[r] = c;
+        if (c > maxc) maxc = c;
+        if (visited[r] == stamp) {
+          if ((size_t)c >= used.size()) used.resize(c + 1, -1);
+          used[c] = stamp;
+        }
+      }
+    }
+    if (n_colors) *n_colors = maxc + 1;
+  } catch (const std::bad_alloc&) {
+    return set_error(TG_ERR_VALUE, "tg_distance2_colors: out of host memory");
+  }
+  return TG_OK;
+}
+
+extern "C" int tg_element_colors(const int32_t* conn, int64_t n_elems, int npe, int64_t n_nodes,
+                                 int32_t* colors, int32_t* order, int32_t* color_ptr,
+                                 int32_t* n_colors) {
+  int rc = check_conn(conn, n_elems, npe, n_nodes);
+  if (rc) return rc;
+  if (!colors || !order || !color_ptr || !n_colors) return set_error(TG_ERR_VALUE, "NULL argument");
+  std::vector<uint64_t> lo(n_nodes, 0), hi(n_nodes, 0);
+  int32_t maxc = -1;
+  for (int64_t e = 0; e < n_elems; ++e) {
+    uint64_t ml = 0, mh = 0;
+    for (int a = 0; a < npe; ++a) {
+      ml |= lo[conn[e * npe + a]];
+      mh |= hi[conn[e * npe + a]];
+    }
+    int c;
+    if (~ml) c = __builtin_ctzll(~ml);
+    else if (~mh) c = 64 + __builtin_ctzll(~mh);
+    else return set_error(TG_ERR_VALUE, "element colouring needs more than 128 colours");
+    colors[e] = c;
+    if (c > maxc) maxc = c;
+    for (int a = 0; a < npe; ++a) {
+      if (c < 64) lo[conn[e * npe + a]] |= (1ULL << c);
+      else hi[conn[e * npe + a]] |= (1ULL << (c - 64));
+    }
+  }
+  const int nc = maxc + 1;
+  std::vector<int32_t> cnt(nc + 1, 0);
+  for (int64_t e = 0; e < n_elems; ++e) cnt[colors[e] + 1]++;
+  for (int c = 0; c < nc; ++c) cnt[c + 1] += cnt[c];
+  for (int c = 0; c <= nc; ++c) color_ptr[c] = cnt[c];
+  for (int64_t e = 0; e < n_elems; ++e) order[cnt[colors[e]]++] = (int32_t)e;
+  *n_colors = nc;
+  return TG_OK;
+}
+
+extern "C" int tg_node_incidence(const int32_t* conn, int64_t n_elems, int npe, int64_t n_nodes,
+                                 int32_t* ptr, int32_t* idx) {
+  int rc = check_conn(conn, n_elems, npe, n_nodes);
+  if (rc) return rc;
+  if (!ptr || (!idx && n_elems > 0)) return set_error(TG_ERR_VALUE, "NULL argument");
+  std::vector<int32_t> p, i;
+  incidence(conn, n_elems, npe, n_nodes, p, i);
+  std::memcpy(ptr, p.data(), p.size() * sizeof(int32_t));
+  if (!i.empty()) std::memcpy(idx, i.data(), i.size() * sizeof(int32_t));
+  return TG_OK;
+}
+
+// ============================================================================ block plan
+extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int64_t n_nodes,
+                             const double* coords, int dim, int block_elems, int max_local_nodes,
+                             void** handle) {
+  if (!handle) return set_error(TG_ERR_VALUE, "handle must not be NULL");
+  *handle = nullptr;
+  int npe, npad;
+  switch (elem) {
+    case TG_TRI3: npe = 3; npad = 4; break;
+    case TG_TET4: npe = 4; npad = 4; break;
+    case TG_HEX8: npe = 8; npad = 8; break;
+    default: return set_error(TG_ERR_VALUE, "unknown element type %d", elem);
+  }
+  if (dim != 2 && dim != 3) return set_error(TG_ERR_VALUE, "dim must be 2 or 3");
+  if (block_elems <= 0) return set_error(TG_ERR_VALUE, "block_elems must be positive");
+  if (max_local_nodes < npe || max_local_nodes > 65535)
+    return set_error(TG_ERR_VALUE, "max_local_nodes must be in [nodes_per_elem, 65535]");
+  int rc = check_conn(conn, n_elems, npe, n_nodes);
+  if (rc) return rc;
+  if (!coords && n_elems > 0) return set_error(TG_ERR_VALUE, "coords must not be NULL");
+  try {
+    auto* P = new Plan();
+    P->npad = npad;
+    P->n_elems = (int32_t)n_elems;
+    // 1. Morton order of element centroids
+    std::vector<std::pair<uint64_t, int32_t>> key(n_elems);
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    std::vector<double> cen(n_elems * dim);
+    for (int64_t e = 0; e < n_elems; ++e)
+      for (int d = 0; d < dim; ++d) {
+        double s = 0;
+        for (int a = 0; a < npe; ++a) s += coords[(int64_t)conn[e * npe + a] * dim + d];
+        s /= npe;
+        cen[e * dim + d] = s;
+        lo[d] = std::min(lo[d], s);
+        hi[d] = std::max(hi[d], s);
+      }
+    const double bits = (dim == 3) ? 2097151.0 : 2147483647.0;
+    for (int64_t e = 0; e < n_elems; ++e) {
+      uint64_t code = 0;
+      for (int d = 0; d < dim; ++d) {
+        const double w = hi[d] - lo[d];
+        const double t = w > 0 ? (cen[e * dim + d] - lo[d]) / w : 0.0;
+        const uint64_t qd = (uint64_t)(t * bits);
+        code |= (dim == 3 ? spread3(qd) : spread2(qd)) << d;
+      }
+      key[e] = {code, (int32_t)e};
+    }
+    cen.clear();
+    cen.shrink_to_fit();
+    std::sort(key.begin(), key.end());
+    // 2. chunk into blocks (element count and local-node cap)
+    std::vector<int32_t> stamp(n_nodes, -1);
+    P->blk_elem_ptr.push_back(0);
+    std::vector<int32_t> blk_nodes;  // local node count per block
+    {
+      int32_t b = 0, ne = 0, nl = 0;
+      for (int64_t k = 0; k < n_elems; ++k) {
+        const int32_t e = key[k].second;
+        int add = 0;  // upper bound on the nodes this element brings into block b
+        for (int a = 0; a < npe; ++a)
+          if (stamp[conn[(int64_t)e * npe + a]] != b) ++add;
+        if (ne > 0 && (ne >= block_elems || nl + add > max_local_nodes)) {
+          P->blk_elem_ptr.push_back((int32_t)k);
+          blk_nodes.push_back(nl);
+          ++b;
+          ne = 0;
+          nl = 0;
+        }
+        for (int a = 0; a < npe; ++a) {
+          const int32_t g = conn[(int64_t)e * npe + a];
+          if (stamp[g] != b) {
+            stamp[g] = b;
+            ++nl;
+          }
+        }
+        ++ne;
+      }
+      if (ne > 0) {
+        P->blk_elem_ptr.push_back((int32_t)n_elems);
+        blk_nodes.push_back(nl);
+      }
+    }
+    const int32_t nb = (int32_t)blk_nodes.size();
+    P->n_blocks = nb;
+    P->blk_node_ptr.assign(nb + 1, 0);
+    for (int32_t b = 0; b < nb; ++b) P->blk_node_ptr[b + 1] = P->blk_node_ptr[b] + blk_nodes[b];
+    const int64_t total_local = P->blk_node_ptr[nb];
+    P->lnode_gid.assign(total_local, 0);
+    P->lnode_slot.assign(total_local, -1);
+    P->elem_id.assign(n_elems, 0);
+    P->lconn.assign(n_elems * npad, 0);
+    // global degree of every node
+    std::vector<int32_t> deg(n_nodes, 0);
+    for (int64_t k = 0; k < n_elems * npe; ++k) deg[conn[k]]++;
+    // 3. per block: local numbering, in-block colouring, shared classification
+    std::vector<std::vector<int32_t>> blk_colors(nb);
+    std::vector<int32_t> blk_nshared(nb, 0);
+    const int nt = nthreads();
+    std::vector<std::vector<int32_t>> lid_t(nt), lcnt_t(nt);
+    std::vector<char> overflow_t(nt, 0);
+    parallel_for(nb, [&](int64_t b0, int64_t b1, int t) {
+      auto& lid = lid_t[t];
+      auto& lcnt = lcnt_t[t];
+      lid.assign(n_nodes, -1);
+      lcnt.assign(n_nodes, 0);
+      std::vector<int32_t> ids, ecol, tmp_e;
+      std::vector<uint16_t> tmp_c;
+      std::vector<uint64_t> mlo, mhi;
+      for (int64_t b = b0; b < b1; ++b) {
+        const int32_t e0 = P->blk_elem_ptr[b], e1 = P->blk_elem_ptr[b + 1];
+        ids.clear();
+        for (int32_t k = e0; k < e1; ++k) {
+          const int32_t e = key[k].second;
+          for (int a = 0; a < npe; ++a) {
+            const int32_t g = conn[(int64_t)e * npe + a];
+            if (lcnt[g]++ == 0) ids.push_back(g);
+          }
+        }
+        std::sort(ids.begin(), ids.end());
+        const int32_t n0 = P->blk_node_ptr[b];
+        for (size_t l = 0; l < ids.size(); ++l) lid[ids[l]] = (int32_t)l;
+        // colouring in Morton order
+        const int32_t ne = e1 - e0;
+        ecol.assign(ne, 0);
+        mlo.assign(ids.size(), 0);
+        mhi.assign(ids.size(), 0);
+        int32_t maxc = -1;
+        for (int32_t k = 0; k < ne; ++k) {
+          const int32_t e = key[e0 + k].second;
+          uint64_t ml = 0, mh = 0;
+          for (int a = 0; a < npe; ++a) {
+            const int32_t l = lid[conn[(int64_t)e * npe + a]];
+            ml |= mlo[l];
+            mh |= mhi[l];
+          }
+          int c;
+          if (~ml) c = __builtin_ctzll(~ml);
+          else if (~mh) c = 64 + __builtin_ctzll(~mh);
+          else { overflow_t[t] = 1; c = 127; }
+          ecol[k] = c;
+          maxc = std::max(maxc, c);
+          for (int a = 0; a < npe; ++a) {
+            const int32_t l = lid[conn[(int64_t)e * npe + a]];
+            if (c < 64) mlo[l] |= 1ULL << c;
+            else mhi[l] |= 1ULL << (c - 64);
+          }
+        }
+        const int nc = maxc + 1;
+        std::vector<int32_t> cofs(nc + 1, 0);
+        for (int32_t k = 0; k < ne; ++k) cofs[ecol[k] + 1]++;
+        for (int c = 0; c < nc; ++c) cofs[c + 1] += cofs[c];
+        blk_colors[b] = cofs;
+        std::vector<int32_t> pos(cofs.begin(), cofs.end() - 1);
+        for (int32_t k = 0; k < ne; ++k) {
+          const int32_t e = key[e0 + k].second;
+          const int32_t dst = e0 + pos[ecol[k]]++;
+          P->elem_id[dst] = e;
+          for (int a = 0; a < npe; ++a)
+            P->lconn[(int64_t)dst * npad + a] = (uint16_t)lid[conn[(int64_t)e * npe + a]];
+          for (int a = npe; a < npad; ++a) P->lconn[(int64_t)dst * npad + a] = 0;
+        }
+        int32_t nsh = 0;
+        for (size_t l = 0; l < ids.size(); ++l) {
+          const int32_t g = ids[l];
+          P->lnode_gid[n0 + l] = g;
+          if (lcnt[g] != deg[g]) {
+            P->lnode_slot[n0 + l] = -2;  // shared: slot assigned below
+            ++nsh;
+          }
+          lcnt[g] = 0;
+          lid[g] = -1;
+        }
+        blk_nshared[b] = nsh;
+      }
+    });
+    lid_t.clear();
+    lcnt_t.clear();
+    for (char o : overflow_t)
+      if (o) {
+        delete P;
+        return set_error(TG_ERR_VALUE, "block colouring needs more than 128 colours; use smaller blocks");
+      }
+    // colour offsets
+    P->blk_color_ptr.assign(nb + 1, 0);
+    for (int32_t b = 0; b < nb; ++b) {
+      P->blk_color_ptr[b + 1] = P->blk_color_ptr[b] + (int32_t)blk_colors[b].size();
+      P->max_colors = std::max<int32_t>(P->max_colors, (int32_t)blk_colors[b].size() - 1);
+      P->max_local = std::max<int32_t>(P->max_local, blk_nodes[b]);
+    }
+    P->color_ofs.reserve(P->blk_color_ptr[nb]);
+    for (int32_t b = 0; b < nb; ++b)
+      P->color_ofs.insert(P->color_ofs.end(), blk_colors[b].begin(), blk_colors[b].end());
+    // 4. partial slots in (block, local node) order, then node -> slots CSR
+    int64_t slot = 0;
+    std::vector<int32_t> nshare(n_nodes, 0);
+    for (int32_t b = 0; b < nb; ++b)
+      for (int32_t l = P->blk_node_ptr[b]; l < P->blk_node_ptr[b + 1]; ++l)
+        if (P->lnode_slot[l] == -2) {
+          P->lnode_slot[l] = (int32_t)slot++;
+          nshare[P->lnode_gid[l]]++;
+        }
+    if (slot > INT32_MAX) {
+      delete P;
+      return set_error(TG_ERR_VALUE, "too many partial slots");
+    }
+    std::vector<int32_t> sidx(n_nodes, -1);
+    for (int64_t g = 0; g < n_nodes; ++g)
+      if (nshare[g] > 0) {
+        sidx[g] = (int32_t)P->shared_node.size();
+        P->shared_node.push_back((int32_t)g);
+      }
+    const int64_t nsh = (int64_t)P->shared_node.size();
+    P->shared_ptr.assign(nsh + 1, 0);
+    for (int64_t s = 0; s < nsh; ++s) P->shared_ptr[s + 1] = P->shared_ptr[s] + nshare[P->shared_node[s]];
+    P->shared_slots.assign(slot, 0);
+    std::vector<int32_t> fill(P->shared_ptr.begin(), P->shared_ptr.end() - 1);
+    for (int32_t b = 0; b < nb; ++b)
+      for (int32_t l = P->blk_node_ptr[b]; l < P->blk_node_ptr[b + 1]; ++l)
+        if (P->lnode_slot[l] >= 0) P->shared_slots[fill[sidx[P->lnode_gid[l]]]++] = P->lnode_slot[l];
+    *handle = P;
+  } catch (const std::bad_alloc&) {
+    return set_error(TG_ERR_VALUE, "tg_plan_build: out of host memory");
+  }
+  return TG_OK;
+}
+
+extern "C" int tg_plan_sizes(const void* handle, int64_t* s) {
+  if (!handle || !s) return set_error(TG_ERR_VALUE, "NULL argument");
+  const Plan* P = static_cast<const Plan*>(handle);
+  s[0] = P->n_blocks;
+  s[1] = P->n_elems;
+  s[2] = (int64_t)P->color_ofs.size();
+  s[3] = (int64_t)P->lnode_gid.size();
+  s[4] = (int64_t)P->shared_node.size();
+  s[5] = (int64_t)P->shared_slots.size();
+  s[6] = P->max_local;
+  s[7] = P->max_colors;
+  s[8] = P->npad;
+  return TG_OK;
+}
+
+extern "C" int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t* blk_color_ptr,
+                              int32_t* color_ofs, int32_t* blk_node_ptr, uint16_t* lconn,
+                              int32_t* elem_id, int32_t* lnode_gid, int32_t* lnode_slot,
+                              int32_t* shared_node, int32_t* shared_ptr, int32_t* shared_slots) {
+  if (!handle) return set_error(TG_ERR_VALUE, "NULL handle");
+  const Plan* P = static_cast<const Plan*>(handle);
+  auto cp = [](auto* dst, const auto& v) {
+    if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+  };
+  cp(blk_elem_ptr, P->blk_elem_ptr);
+  cp(blk_color_ptr, P->blk_color_ptr);
+  cp(color_ofs, P->color_ofs);
+  cp(blk_node_ptr, P->blk_node_ptr);
+  cp(lconn, P->lconn);
+  cp(elem_id, P->elem_id);
+  cp(lnode_gid, P->lnode_gid);
+  cp(lnode_slot, P->lnode_slot);
+  cp(shared_node, P->shared_node);
+  cp(shared_ptr, P->shared_ptr);
+  cp(shared_slots, P->shared_slots);
+  return TG_OK;
+}
+
+extern "C" void tg_plan_free(void* handle) { delete static_cast<Plan*>(handle); }

@@ -1,0 +1,87 @@
+"""Element-block plan on the device (see ``tg_block_plan`` in include/tatva_gb300.h).
+
+Built once per (mesh, element, tuning) on the host by ``tg_plan_build`` and copied
+to the GPU.  The plan fixes the order of every floating-point addition of the
+fused residual / HVP kernels, which makes them deterministic.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+DEFAULT_BLOCK_ELEMS = {_lib.TG_TRI3: 2048, _lib.TG_TET4: 2048, _lib.TG_HEX8: 1024}
+DEFAULT_MAX_LOCAL = 4096
+
+
+class BlockPlan:
+    def __init__(self, elem_id: int, elements: np.ndarray, coords: np.ndarray, device,
+                 block_elems: int | None = None, max_local_nodes: int = DEFAULT_MAX_LOCAL,
+                 threads: int = 256):
+        L = _lib.lib()
+        self.elem = elem_id
+        self.block_elems = int(block_elems or DEFAULT_BLOCK_ELEMS[elem_id])
+        self.max_local_nodes = int(max_local_nodes)
+        conn = np.ascontiguousarray(elements, dtype=np.int32)
+        xyz = np.ascontiguousarray(coords, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _lib.check(L.tg_plan_build(elem_id, conn.ctypes.data, conn.shape[0], xyz.shape[0],
+                                   xyz.ctypes.data, xyz.shape[1], self.block_elems,
+                                   self.max_local_nodes, ctypes.byref(h)))
+        try:
+            sizes = np.zeros(9, dtype=np.int64)
+            _lib.check(L.tg_plan_sizes(h, sizes.ctypes.data))
+            nb, ne, ncol, nloc, nsh, npart, maxl, maxc, npad = (int(x) for x in sizes)
+            host = {
+                "blk_elem_ptr": np.zeros(nb + 1, np.int32),
+                "blk_color_ptr": np.zeros(nb + 1, np.int32),
+                "color_ofs": np.zeros(max(ncol, 1), np.int32),
+                "blk_node_ptr": np.zeros(nb + 1, np.int32),
+                "lconn": np.zeros(max(ne * npad, 8), np.uint16),
+                "elem_id": np.zeros(max(ne, 1), np.int32),
+                "lnode_gid": np.zeros(max(nloc, 1), np.int32),
+                "lnode_slot": np.zeros(max(nloc, 1), np.int32),
+                "shared_node": np.zeros(max(nsh, 1), np.int32),
+                "shared_ptr": np.zeros(nsh + 1, np.int32),
+                "shared_slots": np.zeros(max(npart, 1), np.int32),
+            }
+            order = ["blk_elem_ptr", "blk_color_ptr", "color_ofs", "blk_node_ptr", "lconn",
+                     "elem_id", "lnode_gid", "lnode_slot", "shared_node", "shared_ptr",
+                     "shared_slots"]
+            _lib.check(L.tg_plan_export(h, *[host[k].ctypes.data for k in order]))
+        finally:
+            L.tg_plan_free(h)
+        self.host = host
+        self.sizes = dict(n_blocks=nb, n_elems=ne, color_ofs=ncol, local_nodes=nloc,
+                          n_shared=nsh, n_partials=npart, max_local_nodes=maxl,
+                          max_block_colors=maxc, stride=npad)
+        self.device = torch.device(device)
+        self.dev = {k: torch.from_numpy(v).to(self.device) for k, v in host.items()}
+        s = _lib.BlockPlan()
+        s.n_blocks, s.n_elems, s.nodes_per_elem_padded = nb, ne, npad
+        s.max_local_nodes, s.n_shared, s.n_partials = maxl, nsh, npart
+        s.threads = int(threads)
+        for k in order:
+            setattr(s, k, self.dev[k].data_ptr())
+        self.struct = s
+
+    @property
+    def threads(self) -> int:
+        return int(self.struct.threads)
+
+    @threads.setter
+    def threads(self, t: int) -> None:
+        self.struct.threads = int(t)
+
+    def ref(self):
+        return ctypes.byref(self.struct)
+
+    def stats(self) -> dict:
+        s = dict(self.sizes)
+        s.update(block_elems=self.block_elems, threads=self.threads,
+                 shared_fraction=self.sizes["n_partials"] / max(self.sizes["local_nodes"], 1))
+        return s

@@ -1,0 +1,164 @@
+"""Host-side setup of the C ABI (pattern, colouring, incidence, block plan) against
+the reference goldens and the oracle.  Runs on the CPU (no GPU compute)."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import scipy.sparse as sps
+
+from oracle import mesh as om
+from oracle import sparse as osp
+from tatva_gb300 import Mesh, _lib, sparse
+from tatva_gb300.plan import BlockPlan
+
+MESHES = ["tri", "tet", "hexj", "hexa"]
+
+
+@pytest.mark.parametrize("key", MESHES)
+def test_pattern_and_colors_bit_exact_vs_reference(golden, key):
+    c, e = golden[f"{key}_coords"], golden[f"{key}_elements"]
+    m = Mesh(c, e, device="cpu")
+    for ndpn in ((1, 2, 3) if c.shape[1] == 3 else (1, 2)):
+        csr = sparse.pattern_from_mesh(m, ndpn)
+        assert csr.data.dtype == np.int8 and csr.indices.dtype == np.int32
+        np.testing.assert_array_equal(csr.indptr, golden[f"{key}_pat{ndpn}_indptr"])
+        np.testing.assert_array_equal(csr.indices, golden[f"{key}_pat{ndpn}_indices"])
+        col = sparse.distance2_colors(csr.indptr, csr.indices, csr.shape[0])
+        np.testing.assert_array_equal(col, golden[f"{key}_pat{ndpn}_colors"])
+
+
+def test_mesh_generator_bit_exact_vs_reference(golden):
+    for nx, ny in ((3, 2), (8, 8)):
+        m = Mesh.unit_square(nx, ny, device="cpu")
+        np.testing.assert_array_equal(m.coords.numpy(), golden[f"usq_{nx}x{ny}_coords"])
+        np.testing.assert_array_equal(m.elements.numpy(), golden[f"usq_{nx}x{ny}_elements"])
+
+
+@pytest.mark.parametrize("case", ["tri64", "kuhn6", "brick8", "kuhn_jit5"])
+def test_pattern_and_colors_vs_oracle_larger(case):
+    """Larger meshes than the goldens: C++ setup == numpy restatement, bit for bit."""
+    if case == "tri64":
+        c, e = om.unit_square(64, 64)
+        ndpn, ncol = 1, 9  # configuration-1 mesh: 9 colours
+    elif case == "kuhn6":
+        c, e = om.kuhn_box((1, 1, 1), (6, 6, 6), origin=(0, 0, 0))
+        ndpn, ncol = 3, None
+    elif case == "brick8":
+        c, e = om.brick(8, 8, 8)
+        ndpn, ncol = 3, 81
+    else:
+        c, e = om.kuhn_box((1, 1, 1), (5, 4, 3), origin=(0, 0, 0))
+        ndpn, ncol = 2, None
+    m = Mesh(c, e, device="cpu")
+    csr = sparse.pattern_from_mesh(m, ndpn)
+    ocsr = osp.pattern_from_mesh(c, e, ndpn)
+    np.testing.assert_array_equal(csr.indptr, ocsr.indptr)
+    np.testing.assert_array_equal(csr.indices, ocsr.indices)
+    col = sparse.distance2_colors(csr.indptr, csr.indices, csr.shape[0])
+    if csr.shape[0] <= 6000:
+        ocol = osp.distance2_colors(ocsr.indptr, ocsr.indices, ocsr.shape[0])
+        np.testing.assert_array_equal(col, ocol)
+    assert osp.check_distance2(csr.indptr, csr.indices, col)
+    if ncol is not None:
+        assert col.max() + 1 == ncol
+
+
+def test_coloring_of_general_patterns():
+    """Unsymmetric / irregular CSR input (from_csr accepts any pattern): the grouped
+    C++ greedy equals the row-by-row restatement."""
+    rng = np.random.default_rng(0)
+    for n, dens in ((40, 0.05), (200, 0.02), (300, 0.01)):
+        A = sps.random(n, n, density=dens, random_state=rng, format="csr")
+        A = (A + sps.eye(n)).tocsr()
+        A.sort_indices()
+        # duplicate some rows to exercise the identical-row groups
+        rows = [A.getrow(i) for i in range(n)]
+        for i in range(1, n, 7):
+            rows[i] = rows[i - 1]
+        B = sps.vstack(rows).tocsr()
+        B.sort_indices()
+        col = sparse.distance2_colors(B.indptr, B.indices, n)
+        ocol = osp.distance2_colors(B.indptr, B.indices, n)
+        np.testing.assert_array_equal(col, ocol)
+
+
+def test_colored_matrix_from_csr_host(golden):
+    csr = sparse.pattern_from_mesh(Mesh.unit_square(8, 8, device="cpu"), 2)
+    cm = sparse.ColoredMatrix.from_csr(csr, device="cpu")
+    np.testing.assert_array_equal(cm.colors.numpy(), golden["sq8_pat2_colors"])
+    assert cm.shape == (162, 162) and cm.n_colors == int(golden["sq8_pat2_colors"].max()) + 1
+    back = cm.to_csr()
+    np.testing.assert_array_equal(back.indices, csr.indices)
+
+
+@pytest.mark.parametrize("elem,case,block", [(2, "brick", 512), (2, "brick", 100),
+                                              (1, "kuhn", 777), (0, "tri", 300)])
+def test_block_plan_invariants(elem, case, block):
+    if case == "brick":
+        c, e = om.brick(9, 7, 6)
+        c = om.jitter_interior(c, 0.1, 0.2, seed=0)
+    elif case == "kuhn":
+        c, e = om.kuhn_box((1, 1, 1), (6, 5, 7), origin=(0, 0, 0))
+    else:
+        c, e = om.unit_square(23, 17)
+    p = BlockPlan(elem, e, c, "cpu", block_elems=block, max_local_nodes=4096)
+    h, s = p.host, p.sizes
+    npe, npad = e.shape[1], s["stride"]
+    E = e.shape[0]
+    # every element exactly once
+    np.testing.assert_array_equal(np.sort(h["elem_id"][:E]), np.arange(E))
+    covered_slots = []
+    for b in range(s["n_blocks"]):
+        e0, e1 = h["blk_elem_ptr"][b], h["blk_elem_ptr"][b + 1]
+        n0, n1 = h["blk_node_ptr"][b], h["blk_node_ptr"][b + 1]
+        assert e1 - e0 <= block
+        gid = h["lnode_gid"][n0:n1]
+        assert np.all(np.diff(gid) > 0)  # sorted unique
+        for k in range(e0, e1):
+            lc = h["lconn"][k * npad:k * npad + npe].astype(np.int64)
+            np.testing.assert_array_equal(gid[lc], e[h["elem_id"][k]])
+        # colour classes: no two elements of one colour share a node
+        c0, c1 = h["blk_color_ptr"][b], h["blk_color_ptr"][b + 1]
+        ofs = h["color_ofs"][c0:c1]
+        assert ofs[0] == 0 and ofs[-1] == e1 - e0
+        for a, z in zip(ofs[:-1], ofs[1:]):
+            nodes = np.concatenate([e[h["elem_id"][e0 + k]] for k in range(a, z)])
+            assert len(np.unique(nodes)) == len(nodes)
+        # owned-alone nodes really are touched only by this block
+        slots = h["lnode_slot"][n0:n1]
+        blk_elems = set(h["elem_id"][e0:e1].tolist())
+        for g_, sl in zip(gid, slots):
+            touching = set(np.where((e == g_).any(axis=1))[0].tolist())
+            if sl < 0:
+                assert touching <= blk_elems
+            else:
+                assert not touching <= blk_elems
+                covered_slots.append(sl)
+    # shared-node CSR lists every slot once, in block order
+    assert sorted(covered_slots) == list(range(s["n_partials"]))
+    assert h["shared_ptr"][-1] == s["n_partials"] if s["n_shared"] else True
+
+
+def test_element_colors_and_incidence():
+    c, e = om.kuhn_box((1, 1, 1), (4, 3, 5), origin=(0, 0, 0))
+    E, npe = e.shape
+    L = _lib.lib()
+    colors = np.zeros(E, np.int32)
+    order = np.zeros(E, np.int32)
+    cptr = np.zeros(129, np.int32)
+    nc = ctypes.c_int32()
+    _lib.check(L.tg_element_colors(e.ctypes.data, E, npe, c.shape[0], colors.ctypes.data,
+                                   order.ctypes.data, cptr.ctypes.data, ctypes.byref(nc)))
+    np.testing.assert_array_equal(colors, osp.element_colors(e, c.shape[0]))
+    for k in range(nc.value):
+        sel = order[cptr[k]:cptr[k + 1]]
+        assert np.all(colors[sel] == k) and np.all(np.diff(sel) > 0)
+    ip = np.zeros(c.shape[0] + 1, np.int32)
+    ix = np.zeros(E * npe, np.int32)
+    _lib.check(L.tg_node_incidence(e.ctypes.data, E, npe, c.shape[0], ip.ctypes.data,
+                                   ix.ctypes.data))
+    for n in range(0, c.shape[0], 7):
+        ent = ix[ip[n]:ip[n + 1]]
+        assert np.all(e.reshape(-1)[ent] == n) and np.all(np.diff(ent) > 0)
+        assert len(ent) == np.sum(e == n)

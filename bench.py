@@ -150,45 +150,54 @@ def _dist():
     return ws, rank, local
 
 
-def cpu_hvp_sample(n_cells=32, min_seconds=10.0, processes=1):
-    """Oracle (numpy) HVP of the same law on an n^3 brick: GDOF/s on this host."""
-    from oracle import elements as oe
-    from oracle import materials as omat
-    from oracle import mesh as om
-    from oracle import operator as oop
+class CpuHvp:
+    """Oracle (numpy, FP64) HVP of the same law on an n^3 brick, optionally with the
+    elements split over a pool of worker processes (spawned once)."""
 
-    c, e = om.brick(n_cells, n_cells, n_cells)
-    mu, lm = omat.lame_from_young(1.0, 0.3)
-    law = omat.LinearElastic(mu, lm)
-    v = np.random.default_rng(0).standard_normal(c.shape[0] * 3)
-    if processes > 1:
-        import multiprocessing as mp
+    def __init__(self, n_cells=32, processes=1):
+        from oracle import elements as oe
+        from oracle import materials as omat
+        from oracle import mesh as om
+        from oracle import operator as oop
 
-        chunks = np.array_split(np.arange(e.shape[0]), processes)
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(processes, initializer=_pool_init, initargs=(c, e, law, v)) as pool:
-            pool.map(_pool_hvp, [chunks[0][:8]] * processes)  # warm the workers
-            reps, t0 = 0, time.perf_counter()
-            while True:
-                parts = pool.map(_pool_hvp, chunks)
-                y = np.sum(parts, axis=0)
-                reps += 1
-                if time.perf_counter() - t0 >= min_seconds:
-                    break
-            dt = (time.perf_counter() - t0) / reps
-    else:
-        op = oop.OracleOperator(c, e, oe.Hexahedron8())
-        omat.hvp(op, law, None, v)
+        c, e = om.brick(n_cells, n_cells, n_cells)
+        mu, lm = omat.lame_from_young(1.0, 0.3)
+        self.law = omat.LinearElastic(mu, lm)
+        self.v = np.random.default_rng(0).standard_normal(c.shape[0] * 3)
+        self.ndof = c.shape[0] * 3
+        self.processes = processes
+        self.pool = None
+        if processes > 1:
+            import multiprocessing as mp
+
+            self.chunks = np.array_split(np.arange(e.shape[0]), processes)
+            self.pool = mp.get_context("spawn").Pool(
+                processes, initializer=_pool_init, initargs=(c, e, self.law, self.v))
+        else:
+            self.op = oop.OracleOperator(c, e, oe.Hexahedron8())
+
+    def step(self):
+        from oracle import materials as omat
+
+        if self.pool is not None:
+            return np.sum(self.pool.map(_pool_hvp, self.chunks), axis=0)
+        return omat.hvp(self.op, self.law, None, self.v)
+
+    def measure(self, min_seconds):
+        self.step()
         reps, t0 = 0, time.perf_counter()
         while True:
-            y = omat.hvp(op, law, None, v)
+            self.step()
             reps += 1
             if time.perf_counter() - t0 >= min_seconds:
                 break
         dt = (time.perf_counter() - t0) / reps
-    del y
-    ndof = c.shape[0] * 3
-    return ndof / dt / 1e9, dt, ndof, reps
+        return self.ndof / dt / 1e9, dt, reps
+
+    def close(self):
+        if self.pool is not None:
+            self.pool.close()
+            self.pool.join()
 
 
 _POOL = {}
@@ -214,13 +223,16 @@ def run_reference(args):
         return
     cores = os.cpu_count() or 1
     n = 48
-    vals = []
+    cpu = CpuHvp(n, processes=cores)
+    ndof = cpu.ndof
     for _ in range(args.warmup):
-        cpu_hvp_sample(n, min_seconds=0.0, processes=cores)
+        cpu.step()
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        g, dt, ndof, reps = cpu_hvp_sample(n, min_seconds=0.0, processes=cores)
-        vals.append(g)
-    value = float(np.median(vals))
+        cpu.step()
+    dt = (time.perf_counter() - t0) / args.steps
+    cpu.close()
+    value = ndof / dt / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ndof / value / 1e6,
@@ -336,11 +348,11 @@ def run_ours(args):
         solve = {
             "rtol": 1e-10,
             "fp64": {"seconds": r64.seconds, "iterations": r64.iterations,
-                     "rel_res": r64.rel_res, "converged": r64.converged,
+                     "rel_res": r64.rel_res, "converged": r64.converged, "message": r64.message,
                      "solves_per_s": 1.0 / r64.seconds},
             "mixed": {"seconds": rmx.seconds, "inner_iterations": rmx.iterations,
                       "refinements": rmx.outer, "rel_res": rmx.rel_res,
-                      "converged": rmx.converged, "solves_per_s": 1.0 / rmx.seconds},
+                      "converged": rmx.converged, "message": rmx.message, "solves_per_s": 1.0 / rmx.seconds},
             "speedup_mixed_vs_fp64": r64.seconds / rmx.seconds,
         }
     if ws > 1:
@@ -349,7 +361,9 @@ def run_ours(args):
         return
     cpu = None
     if not args.no_cpu_baseline:
-        gc, dtc, ndc, reps = cpu_hvp_sample(32, min_seconds=args.cpu_seconds, processes=1)
+        cb = CpuHvp(32, processes=1)
+        gc, dtc, reps = cb.measure(args.cpu_seconds)
+        ndc = cb.ndof
         cpu = {"value": gc, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"numpy restatement (FP64) of the HVP on a 32^3 brick ({ndc} dofs), "
                          f"{reps} repetitions, {dtc * 1e3:.1f} ms each"}

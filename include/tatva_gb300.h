@@ -56,6 +56,12 @@ TG_API const char* tg_last_error(void);
 TG_API int tg_version(void);
 /* number of SMs of the current device (0 when no device) */
 TG_API int tg_device_sm_count(void);
+/* Streams of this library's CUDA runtime: for hosts whose stream handles are not
+ * valid in it (the legacy default stream, NULL, is valid everywhere).          */
+TG_API int tg_stream_create(void** stream);
+TG_API int tg_stream_destroy(void* stream);
+TG_API int tg_stream_synchronize(void* stream);
+TG_API int tg_device_synchronize(void);
 
 /* ============================================================================
  * Operator maps (K1-K3).  Replaces tatva/operator.py Operator.eval (:358-377),
@@ -135,7 +141,8 @@ typedef struct tg_block_plan {
   int32_t n_shared;              /* nodes touched by more than one block          */
   int32_t n_partials;            /* partial-sum slots                             */
   int32_t threads;               /* threads per block (64/128/256; 0 = 256)       */
-  int32_t reserved;
+  int32_t n_affine_blocks;       /* Hex8: blocks [0, n_affine_blocks) hold only
+                                    parallelepipeds (exactly, in FP32 and FP64)      */
   const int32_t* blk_elem_ptr;   /* [n_blocks+1] element range of block b         */
   const int32_t* blk_color_ptr;  /* [n_blocks+1] range of b's entries in color_ofs*/
   const int32_t* color_ofs;      /* per block: colour boundaries, relative         */
@@ -166,8 +173,8 @@ typedef struct tg_material {
 TG_API int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int64_t n_nodes,
                   const double* coords, int dim, int block_elems, int max_local_nodes,
                   void** handle);
-/* sizes[0..8] = n_blocks, n_elems, color_ofs_len, total_local_nodes, n_shared,
- * n_partials, max_local_nodes, max_block_colors, stride                          */
+/* sizes[0..9] = n_blocks, n_elems, color_ofs_len, total_local_nodes, n_shared,
+ * n_partials, max_local_nodes, max_block_colors, stride, n_affine_blocks        */
 TG_API int tg_plan_sizes(const void* handle, int64_t* sizes);
 TG_API int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t* blk_color_ptr,
                    int32_t* color_ofs, int32_t* blk_node_ptr, uint16_t* lconn,

@@ -47,6 +47,11 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build tatva_gb300")
 
 
+def _cuda_lib_dir() -> str:
+    nvcc = _nvcc()
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "lib64")
+
+
 def _sources():
     return sorted(
         os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp"))
@@ -65,6 +70,7 @@ def _digest(paths, extra):
         with open(p, "rb") as f:
             h.update(f.read())
     h.update(" ".join(extra).encode())
+    h.update(b"cudart-shared")
     return h.hexdigest()[:16]
 
 
@@ -102,7 +108,11 @@ def build(verbose: bool = False, jobs: int | None = None, extra_flags=()) -> str
     have = open(stamp).read() if os.path.exists(stamp) else None
     if not os.path.exists(LIB_PATH) or have != want or cmds:
         tmp = LIB_PATH + ".tmp"
-        run([nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs, "-lpthread"])
+        # One CUDA runtime per process: link the shared libcudart.so.13 (the one torch
+        # has already loaded resolves it by soname), so that stream handles created by
+        # the host framework are valid in this library.
+        run([nvcc, *ARCH_FLAGS, "-shared", "-cudart", "shared", "-o", tmp, *objs, "-lpthread",
+             "-Xlinker", "-rpath," + _cuda_lib_dir()])
         os.replace(tmp, LIB_PATH)
         with open(stamp, "w") as f:
             f.write(want)

@@ -48,7 +48,7 @@ class BlockPlan(ctypes.Structure):
         ("n_shared", c_int32),
         ("n_partials", c_int32),
         ("threads", c_int32),
-        ("reserved", c_int32),
+        ("n_affine_blocks", c_int32),
         ("blk_elem_ptr", c_void_p),
         ("blk_color_ptr", c_void_p),
         ("color_ofs", c_void_p),
@@ -113,6 +113,10 @@ SIGNATURES = {
     "tg_last_error": (c_char_p, []),
     "tg_version": (c_int, []),
     "tg_device_sm_count": (c_int, []),
+    "tg_stream_create": (I, [POINTER(c_void_p)]),
+    "tg_stream_destroy": (I, [P]),
+    "tg_stream_synchronize": (I, [P]),
+    "tg_device_synchronize": (I, []),
     "tg_eval": (I, [I, I, P, L, I, P, L, P, P]),
     "tg_grad": (I, [I, I, P, P, L, I, P, L, P, P]),
     "tg_integration_weights": (I, [I, I, P, L, P, L, P, P]),
@@ -175,6 +179,8 @@ def lib():
                 f"{os.path.basename(path)} is not built: call tatva_gb300.build() first "
                 "(there is no non-CUDA fallback)"
             )
+        import torch  # noqa: F401  (loads the process's CUDA runtime first)
+
         handle = ctypes.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(handle, name)

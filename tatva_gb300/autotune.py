@@ -19,8 +19,8 @@ _TABLE: dict = {}
 DEFAULT_CANDIDATES = {
     _lib.TG_TRI3: [(1024, 4096, 128), (2048, 4096, 256), (4096, 4096, 256)],
     _lib.TG_TET4: [(1024, 4096, 128), (2048, 4096, 256), (4096, 4096, 256)],
-    _lib.TG_HEX8: [(256, 4096, 64), (512, 4096, 128), (1024, 4096, 128), (1024, 4096, 256),
-                   (2048, 4096, 256)],
+    _lib.TG_HEX8: [(512, 4096, 128), (512, 4096, 256), (1024, 4096, 128), (1024, 4096, 256),
+                   (2048, 4096, 256), (4096, 8192, 256)],
 }
 
 
@@ -51,6 +51,10 @@ def tune(energy, dtype=torch.float32, candidates=None, reps: int = 20, warmup: i
             plan = op.plan(*cfg)
             energy.use_plan(plan)
             y = torch.empty_like(v)
+            try:
+                energy.apply(_lib.TG_MODE_HVP, u, v, out=y)
+            except ValueError:
+                continue  # infeasible (e.g. shared memory) for this law / precision
             for _ in range(warmup):
                 energy.apply(_lib.TG_MODE_HVP, u, v, out=y)
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -63,6 +67,8 @@ def tune(energy, dtype=torch.float32, candidates=None, reps: int = 20, warmup: i
             results.append((s.elapsed_time(e) / reps, cfg, plan.stats()))
     finally:
         energy.use_plan(saved)
+    if not results:
+        raise RuntimeError("no feasible plan among the autotune candidates")
     results.sort(key=lambda r: r[0])
     record(op, results[0][1])
     return [dict(ms=r[0], block_elems=r[1][0], max_local_nodes=r[1][1], threads=r[1][2],

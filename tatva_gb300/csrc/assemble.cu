@@ -23,6 +23,9 @@
 // and the result returns through the transposed transform.  The Gauss rule integrates these
 // products exactly, so the result equals the per-QP evaluation up to rounding, at
 // roughly 1/8 of the flops.  Non-affine elements take the per-QP path.
+#include <map>
+#include <mutex>
+
 #include "tg_common.cuh"
 #include "tg_dispatch.cuh"
 #include "tg_materials.cuh"
@@ -301,34 +304,43 @@ __device__ __forceinline__ void hex_modal_apply(const T (&R)[3][3], T detJm, T m
 }
 
 // ------------------------------------------------------------------ per-element dispatch
-template <int ET, int MAT, class T, int MODE>
+// Kernels instantiated with AFFINE = true run only on blocks whose elements the host
+// verified to be exact parallelepipeds (tg_plan_build replays the coordinate
+// transform below bit for bit in FP32 and FP64); they use the modal evaluation.
+template <int ET, int MAT, int MODE>
+struct HasAffinePath {
+  static constexpr bool value = ET == TG_HEX8 &&
+                                (MAT == TG_LINEAR_ELASTIC || MAT == TG_POISSON) &&
+                                MODE != TG_MODE_DIAG;
+};
+
+template <int ET, int MAT, class T, int MODE, bool AFFINE>
 __device__ __forceinline__ void element_apply(
     T p0, T p1, const T (&X)[Elem<ET>::NN][Elem<ET>::D],
     const T (&U)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V],
     const T (&W)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V],
     T (&Y)[Elem<ET>::NN][LawDims<MAT, Elem<ET>::D>::V]) {
   using E = Elem<ET>;
-  const Law<MAT, E::D, T> law(p0, p1);
-  if constexpr (ET == TG_HEX8 && (MAT == TG_LINEAR_ELASTIC || MAT == TG_POISSON) &&
-                MODE != TG_MODE_DIAG) {
+  if constexpr (AFFINE) {
+    static_assert(HasAffinePath<ET, MAT, MODE>::value, "no affine path for this law / mode");
     T R[3][3], detJm;
-    if (hex_affine_geometry(X, R, detJm)) {
-      const T lam = (MAT == TG_LINEAR_ELASTIC) ? p1 : T(0);
-      if constexpr (MODE == TG_MODE_RESIDUAL) {
-        hex_modal_apply<MAT, T>(R, detJm, p0, lam, U, Y);
-        if constexpr (MAT == TG_POISSON) {
-          // -f int N_a = -f detJ (sum_q N_a(xi_q) = 1 for the 2x2x2 rule)
-          const T fd = p1 * detJm * T(1.0 / 512);
+    hex_affine_geometry(X, R, detJm);
+    const T lam = (MAT == TG_LINEAR_ELASTIC) ? p1 : T(0);
+    if constexpr (MODE == TG_MODE_RESIDUAL) {
+      hex_modal_apply<MAT, T>(R, detJm, p0, lam, U, Y);
+      if constexpr (MAT == TG_POISSON) {
+        // -f int N_a = -f detJ (sum_q N_a(xi_q) = 1 for the 2x2x2 rule)
+        const T fd = p1 * detJm * T(1.0 / 512);
 #pragma unroll
-          for (int a = 0; a < 8; ++a) Y[a][0] -= fd;
-        }
-      } else {
-        hex_modal_apply<MAT, T>(R, detJm, p0, lam, W, Y);
+        for (int a = 0; a < 8; ++a) Y[a][0] -= fd;
       }
-      return;
+    } else {
+      hex_modal_apply<MAT, T>(R, detJm, p0, lam, W, Y);
     }
+  } else {
+    const Law<MAT, E::D, T> law(p0, p1);
+    element_generic<ET, MAT, T, MODE>(law, X, U, W, Y);
   }
-  element_generic<ET, MAT, T, MODE>(law, X, U, W, Y);
 }
 
 // ------------------------------------------------------------------ block kernel
@@ -342,9 +354,9 @@ struct ApplyCfg {
   static constexpr int WORDS_PER_NODE = D + (NEED_U ? V : 0) + (NEED_W ? V : 0) + V;
 };
 
-template <int ET, int MAT, class T, int MODE>
+template <int ET, int MAT, class T, int MODE, bool AFFINE>
 __global__ void __launch_bounds__(APPLY_MAX_THREADS)
-    block_apply_kernel(const tg_block_plan p, const T* __restrict__ coords,
+    block_apply_kernel(const tg_block_plan p, int block0, const T* __restrict__ coords,
                        const T* __restrict__ u, const T* __restrict__ v,
                        const uint8_t* __restrict__ fixed, T* __restrict__ y,
                        T* __restrict__ partials, T p0, T p1, const T* __restrict__ eparam) {
@@ -354,7 +366,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* smem = reinterpret_cast<T*>(smem_raw);
 
-  const int b = blockIdx.x;
+  const int b = block0 + blockIdx.x;
   const int n0 = p.blk_node_ptr[b];
   const int nl = p.blk_node_ptr[b + 1] - n0;
   T* Xs = smem;
@@ -396,7 +408,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
         }
       }
       const T k0 = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
-      element_apply<ET, MAT, T, MODE>(k0, p1, X, U, W, Y);
+      element_apply<ET, MAT, T, MODE, AFFINE>(k0, p1, X, U, W, Y);
 #pragma unroll
       for (int a = 0; a < NN; ++a)
 #pragma unroll
@@ -447,6 +459,204 @@ __global__ void shared_reduce_kernel(const tg_block_plan p, const T* __restrict_
     if (fixed && fixed[dof])
       val = (MODE == TG_MODE_HVP) ? v[dof] : (MODE == TG_MODE_DIAG ? T(1) : T(0));
     y[dof] = val;
+  }
+}
+
+// ------------------------------------------------------------------ affine Hex8 kernel
+// Dedicated kernel for blocks of host-verified parallelepipeds (LE / Poisson, residual
+// or HVP).  Every node occupies one 4-wide slot (x, y, z, 0) / (v0, v1, v2, 0) in
+// shared memory, so each node access is a single 16-byte (FP32) or two 16-byte (FP64)
+// shared-memory operations; slots are XOR-swizzled within groups of 8 to spread the
+// bank quads of the nodes that one quarter-warp touches.  The element geometry comes
+// from the three edge vectors at node 0 (exact for a parallelepiped).
+__device__ __forceinline__ int swz(int l) { return l ^ ((l >> 3) & 7); }
+
+template <class T>
+__device__ __forceinline__ void ld4(const T* p, T& a, T& b, T& c, T& d);
+template <>
+__device__ __forceinline__ void ld4<float>(const float* p, float& a, float& b, float& c,
+                                           float& d) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  a = v.x; b = v.y; c = v.z; d = v.w;
+}
+template <>
+__device__ __forceinline__ void ld4<double>(const double* p, double& a, double& b, double& c,
+                                            double& d) {
+  const double2 v0 = reinterpret_cast<const double2*>(p)[0];
+  const double2 v1 = reinterpret_cast<const double2*>(p)[1];
+  a = v0.x; b = v0.y; c = v1.x; d = v1.y;
+}
+template <class T>
+__device__ __forceinline__ void st4(T* p, T a, T b, T c, T d);
+template <>
+__device__ __forceinline__ void st4<float>(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+template <>
+__device__ __forceinline__ void st4<double>(double* p, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+  reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
+
+template <int MAT, int MODE>
+struct AffineCfg {
+  static constexpr int V = LawDims<MAT, 3>::V;
+  static constexpr int FW = (V == 3) ? 4 : 1;  // words per field slot
+  // X (4) + field (FW) + Y (FW) words per node
+  static constexpr int WORDS_PER_NODE = 4 + 2 * FW;
+};
+
+template <int MAT, class T, int MODE>
+__global__ void __launch_bounds__(APPLY_MAX_THREADS)
+    affine_hex_kernel(const tg_block_plan p, const T* __restrict__ coords,
+                      const T* __restrict__ u, const T* __restrict__ v,
+                      const uint8_t* __restrict__ fixed, T* __restrict__ y,
+                      T* __restrict__ partials, T p0, T p1, const T* __restrict__ eparam) {
+  using C = AffineCfg<MAT, MODE>;
+  constexpr int V = C::V, FW = C::FW;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
+  const int b = blockIdx.x;
+  const int n0 = p.blk_node_ptr[b];
+  const int nl = p.blk_node_ptr[b + 1] - n0;
+  const int nl8 = (nl + 7) & ~7;
+  T* XS = smem;             // nl8 * 4
+  T* FS = XS + nl8 * 4;     // nl8 * FW  (u for the residual, v for the HVP)
+  T* YS = FS + nl8 * FW;    // nl8 * FW
+  const T* fin = (MODE == TG_MODE_RESIDUAL) ? u : v;
+  const int nt = blockDim.x;
+
+  // ---- stage the block's nodes (4 nodes per thread per round, independent loads)
+  for (int l0 = threadIdx.x; l0 < nl; l0 += 4 * nt) {
+    int64_t g[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int l = l0 + k * nt;
+      g[k] = (l < nl) ? (int64_t)__ldg(p.lnode_gid + n0 + l) : 0;
+    }
+    T xv[4][3], fv[4][V];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int l = l0 + k * nt;
+      if (l < nl) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) xv[k][d] = coords[g[k] * 3 + d];
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          const int64_t dof = g[k] * V + i;
+          T val = fin[dof];
+          if (MODE == TG_MODE_HVP && fixed && fixed[dof]) val = T(0);
+          fv[k][i] = val;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int l = l0 + k * nt;
+      if (l < nl) {
+        const int q = swz(l);
+        st4<T>(XS + q * 4, xv[k][0], xv[k][1], xv[k][2], T(0));
+        if constexpr (FW == 4) {
+          st4<T>(FS + q * 4, fv[k][0], fv[k][1], fv[k][2], T(0));
+          st4<T>(YS + q * 4, T(0), T(0), T(0), T(0));
+        } else {
+          FS[q] = fv[k][0];
+          YS[q] = T(0);
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  const T lam = (MAT == TG_LINEAR_ELASTIC) ? p1 : T(0);
+  const int e_base = p.blk_elem_ptr[b];
+  const int c_begin = p.blk_color_ptr[b];
+  const int c_last = p.blk_color_ptr[b + 1] - 1;
+  for (int c = c_begin; c < c_last; ++c) {
+    const int e_end = e_base + p.color_ofs[c + 1];
+    for (int e = e_base + p.color_ofs[c] + threadIdx.x; e < e_end; e += nt) {
+      int lc[8];
+      load_lconn<8>(p.lconn + (int64_t)e * 8, lc);
+      int q[8];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) q[a] = swz(lc[a]);
+      // geometry: Jm = 8 J, rows 4 (x_1 - x_0), 4 (x_3 - x_0), 4 (x_4 - x_0)
+      T Jm[3][3], R[3][3], pad;
+      {
+        T x0[3], xe[3];
+        ld4<T>(XS + q[0] * 4, x0[0], x0[1], x0[2], pad);
+        const int ed[3] = {1, 3, 4};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          ld4<T>(XS + q[ed[i]] * 4, xe[0], xe[1], xe[2], pad);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) Jm[i][k] = T(4) * (xe[k] - x0[k]);
+        }
+      }
+      const T detJm = inv3(Jm, R);
+      T W[8][V], Y[8][V];
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        if constexpr (FW == 4) {
+          ld4<T>(FS + q[a] * 4, W[a][0], W[a][1], W[a][2], pad);
+        } else {
+          W[a][0] = FS[q[a]];
+        }
+      }
+      const T k0 = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
+      hex_modal_apply<MAT, T>(R, detJm, k0, lam, W, Y);
+      if constexpr (MODE == TG_MODE_RESIDUAL && MAT == TG_POISSON) {
+        const T fd = p1 * detJm * T(1.0 / 512);
+#pragma unroll
+        for (int a = 0; a < 8; ++a) Y[a][0] -= fd;
+      }
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        if constexpr (FW == 4) {
+          T y0, y1, y2;
+          ld4<T>(YS + q[a] * 4, y0, y1, y2, pad);
+          st4<T>(YS + q[a] * 4, y0 + Y[a][0], y1 + Y[a][1], y2 + Y[a][2], T(0));
+        } else {
+          YS[q[a]] += Y[a][0];
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- write back: owned-alone nodes to y, shared nodes to their partial slot
+  for (int l0 = threadIdx.x; l0 < nl; l0 += 2 * nt) {
+    int64_t g[2];
+    int slot[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int l = l0 + k * nt;
+      g[k] = (l < nl) ? (int64_t)__ldg(p.lnode_gid + n0 + l) : 0;
+      slot[k] = (l < nl) ? __ldg(p.lnode_slot + n0 + l) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int l = l0 + k * nt;
+      if (l >= nl) continue;
+      T yv[4];
+      if constexpr (FW == 4) {
+        ld4<T>(YS + swz(l) * 4, yv[0], yv[1], yv[2], yv[3]);
+      } else {
+        yv[0] = YS[swz(l)];
+      }
+      if (slot[k] < 0) {
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          const int64_t dof = g[k] * V + i;
+          T val = yv[i];
+          if (fixed && fixed[dof]) val = (MODE == TG_MODE_HVP) ? v[dof] : T(0);
+          y[dof] = val;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < V; ++i) partials[(int64_t)slot[k] * V + i] = yv[i];
+      }
+    }
   }
 }
 
@@ -518,6 +728,34 @@ int dispatch_mode(int mode, F&& f) {
   }
 }
 
+// raise the dynamic shared-memory limit of a kernel once per (kernel, device)
+inline int ensure_smem(const void* fn, size_t smem) {
+  if (smem <= 48 * 1024) return TG_OK;
+  {
+    int dev = 0, optin = 0;
+    TG_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+    TG_TRY(cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+                      "shared memory limit"));
+    if (smem > (size_t)optin)
+      return set_error(TG_ERR_VALUE,
+                       "plan needs %zu bytes of shared memory per block, the device allows %d: "
+                       "build the plan with fewer elements or local nodes per block",
+                       smem, optin);
+  }
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  TG_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  std::lock_guard<std::mutex> g(mu);
+  auto key = std::make_pair(fn, dev);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= smem) return TG_OK;
+  TG_TRY(cuda_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "tg_apply: shared memory attribute"));
+  done[key] = smem;
+  return TG_OK;
+}
+
 inline int plan_check(const tg_block_plan* p, int elem) {
   if (!p) return set_error(TG_ERR_VALUE, "plan must not be NULL");
   if (p->n_blocks < 0 || p->n_elems < 0) return set_error(TG_ERR_VALUE, "corrupt plan");
@@ -575,18 +813,29 @@ extern "C" int tg_apply(int elem, int prec, int mode, const tg_material* mat,
             if (C::NEED_U && !u) return set_error(TG_ERR_VALUE, "u must not be NULL for this mode");
             if (C::NEED_W && !v) return set_error(TG_ERR_VALUE, "v must not be NULL for HVP");
             const size_t smem = (size_t)plan->max_local_nodes * C::WORDS_PER_NODE * sizeof(T);
-            auto kern = block_apply_kernel<ET, MAT, T, MODE>;
-            static size_t configured = 0;
-            if (smem > 48 * 1024 && smem > configured) {
-              TG_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)smem),
-                                "tg_apply: shared memory attribute"));
-              configured = smem;
-            }
             const int threads = plan->threads ? plan->threads : 256;
-            kern<<<plan->n_blocks, threads, smem, st>>>(
-                *plan, (const T*)coords, (const T*)u, (const T*)v, fixed, (T*)y, (T*)workspace,
-                (T)mat->p0, (T)mat->p1, (const T*)mat->elem_param);
+            const int n_aff = HasAffinePath<ET, MAT, MODE>::value ? plan->n_affine_blocks : 0;
+            if (n_aff < 0 || n_aff > plan->n_blocks)
+              return set_error(TG_ERR_VALUE, "plan.n_affine_blocks out of range");
+            if constexpr (HasAffinePath<ET, MAT, MODE>::value) {
+              if (n_aff > 0) {
+                const int nl8 = (plan->max_local_nodes + 7) & ~7;
+                const size_t smem_a = (size_t)nl8 * AffineCfg<MAT, MODE>::WORDS_PER_NODE * sizeof(T);
+                auto ka = affine_hex_kernel<MAT, T, MODE>;
+                TG_TRY(ensure_smem((const void*)ka, smem_a));
+                ka<<<n_aff, threads, smem_a, st>>>(
+                    *plan, (const T*)coords, (const T*)u, (const T*)v, fixed, (T*)y,
+                    (T*)workspace, (T)mat->p0, (T)mat->p1, (const T*)mat->elem_param);
+                TG_TRY(launch_check("tg_apply: affine block kernel"));
+              }
+            }
+            if (plan->n_blocks - n_aff > 0) {
+              auto kg = block_apply_kernel<ET, MAT, T, MODE, false>;
+              TG_TRY(ensure_smem((const void*)kg, smem));
+              kg<<<plan->n_blocks - n_aff, threads, smem, st>>>(
+                  *plan, n_aff, (const T*)coords, (const T*)u, (const T*)v, fixed, (T*)y,
+                  (T*)workspace, (T)mat->p0, (T)mat->p1, (const T*)mat->elem_param);
+            }
             TG_TRY(launch_check("tg_apply: block kernel"));
             if (plan->n_shared > 0) {
               shared_reduce_kernel<T, C::V, MODE><<<grid_for(plan->n_shared, 256), 256, 0, st>>>(

@@ -44,3 +44,26 @@ extern "C" int tg_device_sm_count(void) {
   }
   return n;
 }
+
+// Streams owned by this library's CUDA runtime (for callers whose own stream
+// handles come from another runtime instance).
+extern "C" int tg_stream_create(void** stream) {
+  if (!stream) return tg::set_error(TG_ERR_VALUE, "stream must not be NULL");
+  cudaStream_t s = nullptr;
+  const int rc = tg::cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "tg_stream_create");
+  *stream = rc == TG_OK ? (void*)s : nullptr;
+  return rc;
+}
+
+extern "C" int tg_stream_destroy(void* stream) {
+  if (!stream) return TG_OK;
+  return tg::cuda_check(cudaStreamDestroy((cudaStream_t)stream), "tg_stream_destroy");
+}
+
+extern "C" int tg_stream_synchronize(void* stream) {
+  return tg::cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "tg_stream_synchronize");
+}
+
+extern "C" int tg_device_synchronize(void) {
+  return tg::cuda_check(cudaDeviceSynchronize(), "tg_device_synchronize");
+}

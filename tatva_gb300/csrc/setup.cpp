@@ -79,7 +79,7 @@ struct Pattern {
 };
 
 struct Plan {
-  int32_t n_blocks = 0, n_elems = 0, npad = 4, max_local = 0, max_colors = 0;
+  int32_t n_blocks = 0, n_elems = 0, npad = 4, max_local = 0, max_colors = 0, n_affine = 0;
   std::vector<int32_t> blk_elem_ptr, blk_color_ptr, color_ofs, blk_node_ptr, elem_id, lnode_gid,
       lnode_slot, shared_node, shared_ptr, shared_slots;
   std::vector<uint16_t> lconn;
@@ -102,6 +102,27 @@ uint64_t spread2(uint64_t x) {  // 31 bits -> every second bit
   x = (x | x << 2) & 0x3333333333333333ULL;
   x = (x | x << 1) & 0x5555555555555555ULL;
   return x;
+}
+
+// Exact parallelepiped test of a Hex8 element in precision T, replaying the
+// device's 8-point butterfly on the coordinates (additions only, so the host and
+// the GPU produce identical bits): the bilinear and trilinear modes must vanish.
+template <class T>
+bool hex_affine_exact(const double* coords, const int32_t* nodes) {
+  static const int tmap[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+  for (int k = 0; k < 3; ++k) {
+    volatile T m[8];
+    for (int a = 0; a < 8; ++a) m[tmap[a]] = (T)coords[(int64_t)nodes[a] * 3 + k];
+    for (int h = 1; h < 8; h <<= 1)
+      for (int t = 0; t < 8; ++t)
+        if (!(t & h)) {
+          const T a = m[t], b = m[t | h];
+          m[t] = b + a;
+          m[t | h] = b - a;
+        }
+    if (m[3] != T(0) || m[5] != T(0) || m[6] != T(0) || m[7] != T(0)) return false;
+  }
+  return true;
 }
 
 }  // namespace
@@ -408,6 +429,33 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
     }
     const int32_t nb = (int32_t)blk_nodes.size();
     P->n_blocks = nb;
+    if (elem == TG_HEX8 && dim == 3 && nb > 0) {
+      std::vector<char> aff(nb, 1);
+      parallel_for(nb, [&](int64_t b0, int64_t b1, int) {
+        for (int64_t b = b0; b < b1; ++b)
+          for (int32_t k = P->blk_elem_ptr[b]; k < P->blk_elem_ptr[b + 1] && aff[b]; ++k) {
+            const int32_t* nodes = conn + (int64_t)key[k].second * npe;
+            aff[b] = hex_affine_exact<double>(coords, nodes) && hex_affine_exact<float>(coords, nodes);
+          }
+      });
+      std::vector<int32_t> order;
+      for (int32_t b = 0; b < nb; ++b)
+        if (aff[b]) order.push_back(b);
+      P->n_affine = (int32_t)order.size();
+      for (int32_t b = 0; b < nb; ++b)
+        if (!aff[b]) order.push_back(b);
+      std::vector<std::pair<uint64_t, int32_t>> key2;
+      key2.reserve(n_elems);
+      std::vector<int32_t> ptr2(1, 0), nodes2;
+      for (int32_t b : order) {
+        for (int32_t k = P->blk_elem_ptr[b]; k < P->blk_elem_ptr[b + 1]; ++k) key2.push_back(key[k]);
+        ptr2.push_back((int32_t)key2.size());
+        nodes2.push_back(blk_nodes[b]);
+      }
+      key.swap(key2);
+      P->blk_elem_ptr.swap(ptr2);
+      blk_nodes.swap(nodes2);
+    }
     P->blk_node_ptr.assign(nb + 1, 0);
     for (int32_t b = 0; b < nb; ++b) P->blk_node_ptr[b + 1] = P->blk_node_ptr[b] + blk_nodes[b];
     const int64_t total_local = P->blk_node_ptr[nb];
@@ -562,6 +610,7 @@ extern "C" int tg_plan_sizes(const void* handle, int64_t* s) {
   s[6] = P->max_local;
   s[7] = P->max_colors;
   s[8] = P->npad;
+  s[9] = P->n_affine;
   return TG_OK;
 }
 

@@ -33,9 +33,9 @@ class BlockPlan:
                                    xyz.ctypes.data, xyz.shape[1], self.block_elems,
                                    self.max_local_nodes, ctypes.byref(h)))
         try:
-            sizes = np.zeros(9, dtype=np.int64)
+            sizes = np.zeros(10, dtype=np.int64)
             _lib.check(L.tg_plan_sizes(h, sizes.ctypes.data))
-            nb, ne, ncol, nloc, nsh, npart, maxl, maxc, npad = (int(x) for x in sizes)
+            nb, ne, ncol, nloc, nsh, npart, maxl, maxc, npad, naff = (int(x) for x in sizes)
             host = {
                 "blk_elem_ptr": np.zeros(nb + 1, np.int32),
                 "blk_color_ptr": np.zeros(nb + 1, np.int32),
@@ -58,13 +58,14 @@ class BlockPlan:
         self.host = host
         self.sizes = dict(n_blocks=nb, n_elems=ne, color_ofs=ncol, local_nodes=nloc,
                           n_shared=nsh, n_partials=npart, max_local_nodes=maxl,
-                          max_block_colors=maxc, stride=npad)
+                          max_block_colors=maxc, stride=npad, n_affine_blocks=naff)
         self.device = torch.device(device)
         self.dev = {k: torch.from_numpy(v).to(self.device) for k, v in host.items()}
         s = _lib.BlockPlan()
         s.n_blocks, s.n_elems, s.nodes_per_elem_padded = nb, ne, npad
         s.max_local_nodes, s.n_shared, s.n_partials = maxl, nsh, npart
         s.threads = int(threads)
+        s.n_affine_blocks = naff
         for k in order:
             setattr(s, k, self.dev[k].data_ptr())
         self.struct = s

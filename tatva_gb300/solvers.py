@@ -38,6 +38,7 @@ class SolveResult:
     status: int
     seconds: float
     history: list = field(default_factory=list)
+    message: str = ""
 
     @property
     def converged(self) -> bool:
@@ -67,9 +68,10 @@ def _run(fn, device, raise_on_fail):
     cur.wait_stream(st)
     torch.cuda.synchronize(device)
     dt = time.perf_counter() - t0
+    msg = _lib.lib().tg_last_error().decode(errors="replace") if rc != _lib.TG_OK else ""
     if rc != _lib.TG_OK and raise_on_fail:
-        _lib.check(rc)
-    return stats, rc, dt
+        raise _lib._EXC.get(rc, RuntimeError)(msg)
+    return stats, rc, dt, msg
 
 
 def cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None, fixed=None,
@@ -92,11 +94,11 @@ def cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None, fixed
 
     def go(st, stats):
         return _lib.lib().tg_cg_solve(ctypes.byref(desc), ptr(bb), ptr(x), ptr(diag), rtol,
-                                      int(maxiter), int(check_every), ptr(ws), nb, st, stats)
+                                      int(maxiter), int(check_every), ptr(ws), nb, stats, st)
 
-    stats, rc, dt = _run(go, b.device, raise_on_fail)
+    stats, rc, dt, msg = _run(go, b.device, raise_on_fail)
     del keep
-    return SolveResult(x.view(b.shape), stats.iterations, 0, stats.rel_res, rc, dt)
+    return SolveResult(x.view(b.shape), stats.iterations, 0, stats.rel_res, rc, dt, message=msg)
 
 
 def mixed_cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None, fixed=None,
@@ -119,12 +121,13 @@ def mixed_cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None,
     def go(st, stats):
         return _lib.lib().tg_mixed_solve(ctypes.byref(d64), ctypes.byref(d32), ptr(bb), ptr(x),
                                          ptr(diag), rtol, inner_rtol, int(max_outer),
-                                         int(max_inner), int(check_every), ptr(ws), nb, st,
-                                         stats)
+                                         int(max_inner), int(check_every), ptr(ws), nb, stats,
+                                         st)
 
-    stats, rc, dt = _run(go, b.device, raise_on_fail)
+    stats, rc, dt, msg = _run(go, b.device, raise_on_fail)
     del k64, k32
-    return SolveResult(x.view(b.shape), stats.iterations, stats.outer, stats.rel_res, rc, dt)
+    return SolveResult(x.view(b.shape), stats.iterations, stats.outer, stats.rel_res, rc, dt,
+                       message=msg)
 
 
 def csr_cg(cm, b: torch.Tensor, x0=None, *, fixed=None, rtol: float = 1e-8,
@@ -159,10 +162,10 @@ def csr_cg(cm, b: torch.Tensor, x0=None, *, fixed=None, rtol: float = 1e-8,
 
     def go(st, stats):
         return _lib.lib().tg_cg_solve(ctypes.byref(desc), ptr(bb), ptr(x), ptr(diag), rtol,
-                                      int(maxiter), int(check_every), ptr(ws), nb, st, stats)
+                                      int(maxiter), int(check_every), ptr(ws), nb, stats, st)
 
-    stats, rc, dt = _run(go, b.device, raise_on_fail)
-    return SolveResult(x.view(b.shape), stats.iterations, 0, stats.rel_res, rc, dt)
+    stats, rc, dt, msg = _run(go, b.device, raise_on_fail)
+    return SolveResult(x.view(b.shape), stats.iterations, 0, stats.rel_res, rc, dt, message=msg)
 
 
 def newton(energy, u0: torch.Tensor, lifter, *, colored_matrix=None, rtol: float = 1e-10,

@@ -267,6 +267,8 @@ def run_ours(args):
     en = P["energy"]
     ndof = en.n_dofs
     tune = autotune.tune(en, dtype=torch.float32) if args.autotune else None
+    if not args.autotune and args.block_elems:
+        en.use_plan(P["op"].plan(args.block_elems, 4096, args.threads))
     plan = en.plan()
     g = torch.Generator(device=dev).manual_seed(1234 + rank)
     v = torch.randn(ndof, dtype=torch.float32, device=dev, generator=g)
@@ -402,6 +404,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_CELLS)
     ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--block-elems", type=int, default=0, help="plan when --autotune 0")
+    ap.add_argument("--threads", type=int, default=256, help="plan when --autotune 0")
     ap.add_argument("--solve", type=int, default=1)
     ap.add_argument("--max-iter", type=int, default=20000)
     ap.add_argument("--inner-rtol", type=float, default=1e-4)

@@ -28,6 +28,7 @@
 
 #include "tg_common.cuh"
 #include "tg_dispatch.cuh"
+#include "tg_internal.h"
 #include "tg_materials.cuh"
 
 namespace tg {
@@ -219,6 +220,33 @@ __device__ __forceinline__ void modal_flux(const T (&R)[3][3], const T (&G)[3][V
     }
 }
 
+// Linear elasticity, monomial carried by two reference directions p < q with
+// coefficient vectors gp, gq (over components): with r_a = R[:, a] and the metric
+// Gm = R^T R,  F_p = sigma r_p,  F_q = sigma r_q  where
+// sigma = mu (H + H^T) + lam tr(H) I,  H = gp r_p^T + gq r_q^T, written out through
+// the dot products g.r and Gm (no 3x3 products).
+template <class T, int P, int Q>
+__device__ __forceinline__ void le_two_dir(const T (&R)[3][3], const T (&Gm)[3][3],
+                                           const T (&gp)[3], const T (&gq)[3], T mu, T lam,
+                                           T (&Fp)[3], T (&Fq)[3]) {
+  T a_pp = T(0), a_pq = T(0), a_qp = T(0), a_qq = T(0);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    a_pp += gp[k] * R[k][P];
+    a_pq += gp[k] * R[k][Q];
+    a_qp += gq[k] * R[k][P];
+    a_qq += gq[k] * R[k][Q];
+  }
+  const T lt = lam * (a_pp + a_qq);
+  const T c1 = mu * Gm[P][P], c2 = mu * Gm[P][Q], c3 = mu * a_pp + lt, c4 = mu * a_qp;
+  const T d2 = mu * Gm[Q][Q], d3 = mu * a_pq, d4 = mu * a_qq + lt;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    Fp[j] = c1 * gp[j] + c2 * gq[j] + c3 * R[j][P] + c4 * R[j][Q];
+    Fq[j] = c2 * gp[j] + d2 * gq[j] + d3 * R[j][P] + d4 * R[j][Q];
+  }
+}
+
 // y = dE/du for psi quadratic in grad u (LE: mu, lam; Poisson: kappa in mu), affine hex.
 // W holds the nodal values the quadratic form acts on.  Returns the element
 // Jacobian determinant (unscaled: det(8 J)).
@@ -253,47 +281,101 @@ __device__ __forceinline__ void hex_modal_apply(const T (&R)[3][3], T detJm, T m
       dM[j][4] = F[j][2];
     }
   }
+  if constexpr (MAT == TG_LINEAR_ELASTIC) {
+    T Gm[3][3];
+#pragma unroll
+    for (int a2 = 0; a2 < 3; ++a2)
+#pragma unroll
+      for (int b2 = a2; b2 < 3; ++b2) {
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc += R[k][a2] * R[k][b2];
+        Gm[a2][b2] = acc;
+        Gm[b2][a2] = acc;
+      }
+    const T mu1 = mu * s1, lam1 = lam * s1;
+    T g12[3], g13[3], g23[3], g123[3], Fp[3], Fq[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      g12[j] = M[j][3];
+      g13[j] = M[j][5];
+      g23[j] = M[j][6];
+      g123[j] = M[j][7];
+    }
+    // monomial x: directions (y, z) carry (M12, M13)
+    le_two_dir<T, 1, 2>(R, Gm, g12, g13, mu1, lam1, Fp, Fq);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { dM[j][3] = Fp[j]; dM[j][5] = Fq[j]; }
+    // monomial y: directions (x, z) carry (M12, M23)
+    le_two_dir<T, 0, 2>(R, Gm, g12, g23, mu1, lam1, Fp, Fq);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { dM[j][3] += Fp[j]; dM[j][6] = Fq[j]; }
+    // monomial z: directions (x, y) carry (M13, M23)
+    le_two_dir<T, 0, 1>(R, Gm, g13, g23, mu1, lam1, Fp, Fq);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { dM[j][5] += Fp[j]; dM[j][6] += Fq[j]; }
+    // monomials yz, xz, xy (direction x, y, z carries M123):
+    // sum_i [mu Gm_ii g + (mu + lam)(g.r_i) r_i] = mu tr(Gm) g + (mu + lam) R R^T g
+    const T mu2 = mu * s2, ml2 = (mu + lam) * s2;
+    const T trG = Gm[0][0] + Gm[1][1] + Gm[2][2];
+    T h[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) acc += R[k][i] * g123[k];
+      h[i] = acc;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T acc = T(0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) acc += R[j][i] * h[i];
+      dM[j][7] = mu2 * trG * g123[j] + ml2 * acc;
+    }
+  } else {
   {  // monomial x: directions (y, z) carry (M12, M13)
-    T G[3][V], F[V][3];
-#pragma unroll
-    for (int j = 0; j < V; ++j) { G[0][j] = T(0); G[1][j] = M[j][3]; G[2][j] = M[j][5]; }
-    modal_flux<T, 6, V, MAT>(R, G, mu * s1, lam * s1, F);
-#pragma unroll
-    for (int j = 0; j < V; ++j) { dM[j][3] = F[j][1]; dM[j][5] = F[j][2]; }
-  }
-  {  // monomial y: directions (x, z) carry (M12, M23)
-    T G[3][V], F[V][3];
-#pragma unroll
-    for (int j = 0; j < V; ++j) { G[0][j] = M[j][3]; G[1][j] = T(0); G[2][j] = M[j][6]; }
-    modal_flux<T, 5, V, MAT>(R, G, mu * s1, lam * s1, F);
-#pragma unroll
-    for (int j = 0; j < V; ++j) { dM[j][3] += F[j][0]; dM[j][6] = F[j][2]; }
-  }
-  {  // monomial z: directions (x, y) carry (M13, M23)
-    T G[3][V], F[V][3];
-#pragma unroll
-    for (int j = 0; j < V; ++j) { G[0][j] = M[j][5]; G[1][j] = M[j][6]; G[2][j] = T(0); }
-    modal_flux<T, 3, V, MAT>(R, G, mu * s1, lam * s1, F);
-#pragma unroll
-    for (int j = 0; j < V; ++j) { dM[j][5] += F[j][0]; dM[j][6] += F[j][1]; }
-  }
-  {  // monomials yz, xz, xy: direction x, y, z carries M123
-    T G[3][V], F[V][3];
-#pragma unroll
-    for (int j = 0; j < V; ++j) { G[0][j] = M[j][7]; G[1][j] = T(0); G[2][j] = T(0); }
-    modal_flux<T, 1, V, MAT>(R, G, mu * s2, lam * s2, F);
-#pragma unroll
-    for (int j = 0; j < V; ++j) dM[j][7] = F[j][0];
-#pragma unroll
-    for (int j = 0; j < V; ++j) { G[0][j] = T(0); G[1][j] = M[j][7]; }
-    modal_flux<T, 2, V, MAT>(R, G, mu * s2, lam * s2, F);
-#pragma unroll
-    for (int j = 0; j < V; ++j) dM[j][7] += F[j][1];
-#pragma unroll
-    for (int j = 0; j < V; ++j) { G[1][j] = T(0); G[2][j] = M[j][7]; }
-    modal_flux<T, 4, V, MAT>(R, G, mu * s2, lam * s2, F);
-#pragma unroll
-    for (int j = 0; j < V; ++j) dM[j][7] += F[j][2];
+      T G[3][V], F[V][3];
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { G[0][j] = T(0); G[1][j] = M[j][3]; G[2][j] = M[j][5]; }
+      modal_flux<T, 6, V, MAT>(R, G, mu * s1, lam * s1, F);
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { dM[j][3] = F[j][1]; dM[j][5] = F[j][2]; }
+    }
+    {  // monomial y: directions (x, z) carry (M12, M23)
+      T G[3][V], F[V][3];
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { G[0][j] = M[j][3]; G[1][j] = T(0); G[2][j] = M[j][6]; }
+      modal_flux<T, 5, V, MAT>(R, G, mu * s1, lam * s1, F);
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { dM[j][3] += F[j][0]; dM[j][6] = F[j][2]; }
+    }
+    {  // monomial z: directions (x, y) carry (M13, M23)
+      T G[3][V], F[V][3];
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { G[0][j] = M[j][5]; G[1][j] = M[j][6]; G[2][j] = T(0); }
+      modal_flux<T, 3, V, MAT>(R, G, mu * s1, lam * s1, F);
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { dM[j][5] += F[j][0]; dM[j][6] += F[j][1]; }
+    }
+    {  // monomials yz, xz, xy: direction x, y, z carries M123
+      T G[3][V], F[V][3];
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { G[0][j] = M[j][7]; G[1][j] = T(0); G[2][j] = T(0); }
+      modal_flux<T, 1, V, MAT>(R, G, mu * s2, lam * s2, F);
+  #pragma unroll
+      for (int j = 0; j < V; ++j) dM[j][7] = F[j][0];
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { G[0][j] = T(0); G[1][j] = M[j][7]; }
+      modal_flux<T, 2, V, MAT>(R, G, mu * s2, lam * s2, F);
+  #pragma unroll
+      for (int j = 0; j < V; ++j) dM[j][7] += F[j][1];
+  #pragma unroll
+      for (int j = 0; j < V; ++j) { G[1][j] = T(0); G[2][j] = M[j][7]; }
+      modal_flux<T, 4, V, MAT>(R, G, mu * s2, lam * s2, F);
+  #pragma unroll
+      for (int j = 0; j < V; ++j) dM[j][7] += F[j][2];
+    }
   }
 #pragma unroll
   for (int j = 0; j < V; ++j) {
@@ -568,16 +650,24 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   }
   __syncthreads();
 
+  // ---- elements: every thread computes one element of the current chunk into
+  // registers (no barrier), then the chunk's results are added into shared memory
+  // one element colour at a time (elements of a colour share no node), so the
+  // order of the additions at every node is the plan's colour order.
   const T lam = (MAT == TG_LINEAR_ELASTIC) ? p1 : T(0);
   const int e_base = p.blk_elem_ptr[b];
+  const int ne = p.blk_elem_ptr[b + 1] - e_base;
   const int c_begin = p.blk_color_ptr[b];
   const int c_last = p.blk_color_ptr[b + 1] - 1;
-  for (int c = c_begin; c < c_last; ++c) {
-    const int e_end = e_base + p.color_ofs[c + 1];
-    for (int e = e_base + p.color_ofs[c] + threadIdx.x; e < e_end; e += nt) {
+  for (int k0 = 0; k0 < ne; k0 += nt) {
+    const int k = k0 + threadIdx.x;
+    const bool act = k < ne;
+    T Y[8][V];
+    int q[8];
+    if (act) {
+      const int e = e_base + k;
       int lc[8];
       load_lconn<8>(p.lconn + (int64_t)e * 8, lc);
-      int q[8];
 #pragma unroll
       for (int a = 0; a < 8; ++a) q[a] = swz(lc[a]);
       // geometry: Jm = 8 J, rows 4 (x_1 - x_0), 4 (x_3 - x_0), 4 (x_4 - x_0)
@@ -590,11 +680,11 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
         for (int i = 0; i < 3; ++i) {
           ld4<T>(XS + q[ed[i]] * 4, xe[0], xe[1], xe[2], pad);
 #pragma unroll
-          for (int k = 0; k < 3; ++k) Jm[i][k] = T(4) * (xe[k] - x0[k]);
+          for (int d = 0; d < 3; ++d) Jm[i][d] = T(4) * (xe[d] - x0[d]);
         }
       }
       const T detJm = inv3(Jm, R);
-      T W[8][V], Y[8][V];
+      T W[8][V];
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
         if constexpr (FW == 4) {
@@ -603,25 +693,32 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
           W[a][0] = FS[q[a]];
         }
       }
-      const T k0 = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
-      hex_modal_apply<MAT, T>(R, detJm, k0, lam, W, Y);
+      const T k0p = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
+      hex_modal_apply<MAT, T>(R, detJm, k0p, lam, W, Y);
       if constexpr (MODE == TG_MODE_RESIDUAL && MAT == TG_POISSON) {
         const T fd = p1 * detJm * T(1.0 / 512);
 #pragma unroll
         for (int a = 0; a < 8; ++a) Y[a][0] -= fd;
       }
+    }
+    for (int c = c_begin; c < c_last; ++c) {
+      const int lo = max(p.color_ofs[c], k0);
+      const int hi = min(p.color_ofs[c + 1], k0 + nt);
+      if (lo >= hi) continue;  // the same decision in every thread of the block
+      if (act && k >= lo && k < hi) {
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
-        if constexpr (FW == 4) {
-          T y0, y1, y2;
-          ld4<T>(YS + q[a] * 4, y0, y1, y2, pad);
-          st4<T>(YS + q[a] * 4, y0 + Y[a][0], y1 + Y[a][1], y2 + Y[a][2], T(0));
-        } else {
-          YS[q[a]] += Y[a][0];
+        for (int a = 0; a < 8; ++a) {
+          if constexpr (FW == 4) {
+            T y0, y1, y2, pad;
+            ld4<T>(YS + q[a] * 4, y0, y1, y2, pad);
+            st4<T>(YS + q[a] * 4, y0 + Y[a][0], y1 + Y[a][1], y2 + Y[a][2], T(0));
+          } else {
+            YS[q[a]] += Y[a][0];
+          }
         }
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
 
   // ---- write back: owned-alone nodes to y, shared nodes to their partial slot
@@ -818,7 +915,18 @@ extern "C" int tg_apply(int elem, int prec, int mode, const tg_material* mat,
             if (n_aff < 0 || n_aff > plan->n_blocks)
               return set_error(TG_ERR_VALUE, "plan.n_affine_blocks out of range");
             if constexpr (HasAffinePath<ET, MAT, MODE>::value) {
-              if (n_aff > 0) {
+              bool done = false;
+              if constexpr (std::is_same<T, float>::value && MAT == TG_LINEAR_ELASTIC) {
+                if (n_aff > 0 && mat->elem_param == nullptr) {
+                  const int rc5 = launch_hex_le_f32x2(plan, MODE, (const float*)coords,
+                                                      (const float*)u, (const float*)v, fixed,
+                                                      (float*)y, (float*)workspace,
+                                                      (float)mat->p0, (float)mat->p1, st);
+                  if (rc5 == TG_OK) done = true;
+                  else if (rc5 != TG_ERR_UNSUPPORTED) return rc5;
+                }
+              }
+              if (n_aff > 0 && !done) {
                 const int nl8 = (plan->max_local_nodes + 7) & ~7;
                 const size_t smem_a = (size_t)nl8 * AffineCfg<MAT, MODE>::WORDS_PER_NODE * sizeof(T);
                 auto ka = affine_hex_kernel<MAT, T, MODE>;

@@ -1,0 +1,19 @@
+// Entry points shared between translation units of the library (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "tatva_gb300.h"
+
+namespace tg {
+
+// FP32 linear-elastic Hex8 residual / HVP over the plan's all-parallelepiped blocks
+// [0, n_affine_blocks); returns TG_ERR_UNSUPPORTED (nothing launched) when the plan
+// does not fit the kernel's staging limits.
+int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords, const float* u,
+                        const float* v, const uint8_t* fixed, float* y, float* partials,
+                        float mu, float lam, cudaStream_t st);
+
+}  // namespace tg

@@ -147,6 +147,27 @@ def test_hex_brick_affine_and_general(cuda, shape, jitter, kind):
                omat.hvp(oo, law, u, v)) < 1e-4
 
 
+@pytest.mark.parametrize("kind", ["linear_elastic", "poisson"])
+def test_hex_sheared_parallelepipeds_modal_path(cuda, kind):
+    """A sheared brick with dyadic shear factors: every element is an exact
+    parallelepiped in FP32 and FP64, so all blocks take the modal kernel with a full
+    (non-diagonal) Jacobian."""
+    c, e = om.brick(6, 5, 7, lengths=(6.0, 5.0, 7.0))  # integer grid
+    A = np.array([[1.0, 0.25, -0.125], [0.5, 1.0, 0.25], [0.0, -0.375, 1.0]]) / 8
+    c = c @ A.T  # dyadic shear: exact in FP32 and FP64
+    op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    assert op.plan().sizes["n_affine_blocks"] == op.plan().sizes["n_blocks"]
+    oo = oop.OracleOperator(c, e, oe.Hexahedron8())
+    en, law = {"linear_elastic": (materials.LinearElastic(op, 0.7, 1.9), omat.LinearElastic(0.7, 1.9)),
+               "poisson": (materials.Poisson(op, 1.3, 0.6), omat.Poisson(1.3, 0.6))}[kind]
+    rng = np.random.default_rng(2)
+    n = c.shape[0] * en.n_values
+    u, v = rng.standard_normal(n), rng.standard_normal(n)
+    assert rel(en.residual(_t(u, cuda)), omat.residual(oo, law, u)) < F64_TOL
+    assert rel(en.hvp(None, _t(v, cuda)), omat.hvp(oo, law, u, v)) < F64_TOL
+    assert rel(en.hvp(None, _t(v, cuda, torch.float32)), omat.hvp(oo, law, u, v)) < 1e-5
+
+
 def test_unit_square_poisson_c1_size(cuda):
     """Configuration-1 size (64x64 Tri3, f=1): residual of u and HVP vs the oracle."""
     c, e = om.unit_square(64, 64)

@@ -143,6 +143,9 @@ typedef struct tg_block_plan {
   int32_t threads;               /* threads per block (64/128/256; 0 = 256)       */
   int32_t n_affine_blocks;       /* Hex8: blocks [0, n_affine_blocks) hold only
                                     parallelepipeds (exactly, in FP32 and FP64)      */
+  int32_t n_diag_blocks;         /* Hex8: blocks [0, n_diag_blocks) hold only
+                                    axis-aligned boxes (a prefix of the affine ones) */
+  int32_t max_block_elems;       /* largest element count of a block                */
   const int32_t* blk_elem_ptr;   /* [n_blocks+1] element range of block b         */
   const int32_t* blk_color_ptr;  /* [n_blocks+1] range of b's entries in color_ofs*/
   const int32_t* color_ofs;      /* per block: colour boundaries, relative         */
@@ -151,6 +154,7 @@ typedef struct tg_block_plan {
   const int32_t* elem_id;        /* [n_elems] original element id                  */
   const int32_t* lnode_gid;      /* [sum L_b] global node id                       */
   const int32_t* lnode_slot;     /* [sum L_b] -1: owned alone, else partial slot   */
+  const int32_t* lnode_smem;     /* [sum L_b] shared-memory slot of the local node */
   const int32_t* shared_node;    /* [n_shared] global node id                      */
   const int32_t* shared_ptr;     /* [n_shared+1]                                   */
   const int32_t* shared_slots;   /* [n_partials] slots in summation order          */
@@ -173,13 +177,17 @@ typedef struct tg_material {
 TG_API int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int64_t n_nodes,
                   const double* coords, int dim, int block_elems, int max_local_nodes,
                   void** handle);
-/* sizes[0..9] = n_blocks, n_elems, color_ofs_len, total_local_nodes, n_shared,
- * n_partials, max_local_nodes, max_block_colors, stride, n_affine_blocks        */
+/* sizes[0..11] = n_blocks, n_elems, color_ofs_len, total_local_nodes, n_shared,
+ * n_partials, max_local_nodes, max_block_colors, stride, n_affine_blocks,
+ * n_diag_blocks, max_block_elems.  Local node l of a block lives in shared-memory
+ * slot lnode_smem[l] < 8 ceil(L_b / 8), chosen so that the nodes one quarter-warp
+ * reads at an element corner fall in distinct bank quads; lconn stores slots.   */
 TG_API int tg_plan_sizes(const void* handle, int64_t* sizes);
 TG_API int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t* blk_color_ptr,
                    int32_t* color_ofs, int32_t* blk_node_ptr, uint16_t* lconn,
                    int32_t* elem_id, int32_t* lnode_gid, int32_t* lnode_slot,
-                   int32_t* shared_node, int32_t* shared_ptr, int32_t* shared_slots);
+                   int32_t* lnode_smem, int32_t* shared_node, int32_t* shared_ptr,
+                   int32_t* shared_slots);
 TG_API void tg_plan_free(void* handle);
 
 /* y = mode(u, v) over the plan:

@@ -49,6 +49,8 @@ class BlockPlan(ctypes.Structure):
         ("n_partials", c_int32),
         ("threads", c_int32),
         ("n_affine_blocks", c_int32),
+        ("n_diag_blocks", c_int32),
+        ("max_block_elems", c_int32),
         ("blk_elem_ptr", c_void_p),
         ("blk_color_ptr", c_void_p),
         ("color_ofs", c_void_p),
@@ -57,6 +59,7 @@ class BlockPlan(ctypes.Structure):
         ("elem_id", c_void_p),
         ("lnode_gid", c_void_p),
         ("lnode_slot", c_void_p),
+        ("lnode_smem", c_void_p),
         ("shared_node", c_void_p),
         ("shared_ptr", c_void_p),
         ("shared_slots", c_void_p),
@@ -130,7 +133,7 @@ SIGNATURES = {
     "tg_eval_transpose": (I, [I, I, P, L, I, P, L, P, P, P, P]),
     "tg_plan_build": (I, [I, P, L, L, P, I, I, I, POINTER(c_void_p)]),
     "tg_plan_sizes": (I, [P, P]),
-    "tg_plan_export": (I, [P] + [P] * 11),
+    "tg_plan_export": (I, [P] + [P] * 12),
     "tg_plan_free": (None, [P]),
     "tg_apply_workspace_bytes": (S, [I, I, I, P]),
     "tg_apply": (I, [I, I, I, P, P, P, L, P, P, P, P, P, S, P]),

@@ -35,6 +35,8 @@ namespace tg {
 
 constexpr int APPLY_MAX_THREADS = 256;
 
+
+
 template <int ET, int MAT>
 struct Supported {
   static constexpr bool value = !(MAT == TG_NEO_HOOKEAN && Elem<ET>::D != 3);
@@ -451,21 +453,23 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   const int b = block0 + blockIdx.x;
   const int n0 = p.blk_node_ptr[b];
   const int nl = p.blk_node_ptr[b + 1] - n0;
+  const int nl8 = (nl + 7) & ~7;  // local node l lives in shared-memory slot lnode_smem[l] < nl8
   T* Xs = smem;
-  T* Us = Xs + nl * D;
-  T* Ws = Us + (C::NEED_U ? nl * V : 0);
-  T* Ys = Ws + (C::NEED_W ? nl * V : 0);
+  T* Us = Xs + nl8 * D;
+  T* Ws = Us + (C::NEED_U ? nl8 * V : 0);
+  T* Ys = Ws + (C::NEED_W ? nl8 * V : 0);
 
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {
     const int64_t g = __ldg(p.lnode_gid + n0 + l);
+    const int q = __ldg(p.lnode_smem + n0 + l);
 #pragma unroll
-    for (int d = 0; d < D; ++d) Xs[l * D + d] = coords[g * D + d];
+    for (int d = 0; d < D; ++d) Xs[q * D + d] = coords[g * D + d];
 #pragma unroll
     for (int i = 0; i < V; ++i) {
       const int64_t dof = g * V + i;
-      if constexpr (C::NEED_U) Us[l * V + i] = u[dof];
-      if constexpr (C::NEED_W) Ws[l * V + i] = (fixed && fixed[dof]) ? T(0) : v[dof];
-      Ys[l * V + i] = T(0);
+      if constexpr (C::NEED_U) Us[q * V + i] = u[dof];
+      if constexpr (C::NEED_W) Ws[q * V + i] = (fixed && fixed[dof]) ? T(0) : v[dof];
+      Ys[q * V + i] = T(0);
     }
   }
   __syncthreads();
@@ -502,18 +506,19 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {
     const int64_t g = __ldg(p.lnode_gid + n0 + l);
     const int slot = __ldg(p.lnode_slot + n0 + l);
+    const int q = __ldg(p.lnode_smem + n0 + l);
     if (slot < 0) {
 #pragma unroll
       for (int i = 0; i < V; ++i) {
         const int64_t dof = g * V + i;
-        T val = Ys[l * V + i];
+        T val = Ys[q * V + i];
         if (fixed && fixed[dof])
           val = (MODE == TG_MODE_HVP) ? v[dof] : (MODE == TG_MODE_DIAG ? T(1) : T(0));
         y[dof] = val;
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < V; ++i) partials[(int64_t)slot * V + i] = Ys[l * V + i];
+      for (int i = 0; i < V; ++i) partials[(int64_t)slot * V + i] = Ys[q * V + i];
     }
   }
 }
@@ -551,7 +556,6 @@ __global__ void shared_reduce_kernel(const tg_block_plan p, const T* __restrict_
 // shared-memory operations; slots are XOR-swizzled within groups of 8 to spread the
 // bank quads of the nodes that one quarter-warp touches.  The element geometry comes
 // from the three edge vectors at node 0 (exact for a parallelepiped).
-__device__ __forceinline__ int swz(int l) { return l ^ ((l >> 3) & 7); }
 
 template <class T>
 __device__ __forceinline__ void ld4(const T* p, T& a, T& b, T& c, T& d);
@@ -636,7 +640,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
     for (int k = 0; k < 4; ++k) {
       const int l = l0 + k * nt;
       if (l < nl) {
-        const int q = swz(l);
+        const int q = __ldg(p.lnode_smem + n0 + l);
         st4<T>(XS + q * 4, xv[k][0], xv[k][1], xv[k][2], T(0));
         if constexpr (FW == 4) {
           st4<T>(FS + q * 4, fv[k][0], fv[k][1], fv[k][2], T(0));
@@ -669,7 +673,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
       int lc[8];
       load_lconn<8>(p.lconn + (int64_t)e * 8, lc);
 #pragma unroll
-      for (int a = 0; a < 8; ++a) q[a] = swz(lc[a]);
+      for (int a = 0; a < 8; ++a) q[a] = lc[a];
       // geometry: Jm = 8 J, rows 4 (x_1 - x_0), 4 (x_3 - x_0), 4 (x_4 - x_0)
       T Jm[3][3], R[3][3], pad;
       {
@@ -736,10 +740,11 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
       const int l = l0 + k * nt;
       if (l >= nl) continue;
       T yv[4];
+      const int ql = __ldg(p.lnode_smem + n0 + l);
       if constexpr (FW == 4) {
-        ld4<T>(YS + swz(l) * 4, yv[0], yv[1], yv[2], yv[3]);
+        ld4<T>(YS + ql * 4, yv[0], yv[1], yv[2], yv[3]);
       } else {
-        yv[0] = YS[swz(l)];
+        yv[0] = YS[ql];
       }
       if (slot[k] < 0) {
 #pragma unroll
@@ -909,7 +914,8 @@ extern "C" int tg_apply(int elem, int prec, int mode, const tg_material* mat,
             using C = ApplyCfg<ET, MAT, T, MODE>;
             if (C::NEED_U && !u) return set_error(TG_ERR_VALUE, "u must not be NULL for this mode");
             if (C::NEED_W && !v) return set_error(TG_ERR_VALUE, "v must not be NULL for HVP");
-            const size_t smem = (size_t)plan->max_local_nodes * C::WORDS_PER_NODE * sizeof(T);
+            const size_t smem =
+                (size_t)((plan->max_local_nodes + 7) & ~7) * C::WORDS_PER_NODE * sizeof(T);
             const int threads = plan->threads ? plan->threads : 256;
             const int n_aff = HasAffinePath<ET, MAT, MODE>::value ? plan->n_affine_blocks : 0;
             if (n_aff < 0 || n_aff > plan->n_blocks)

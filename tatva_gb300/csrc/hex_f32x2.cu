@@ -1,32 +1,35 @@
 // FP32 linear-elastic Hex8 residual / HVP on blocks of exact parallelepipeds:
-// persistent CTAs, two-stage cp.async pipeline, two elements per thread in packed
-// f32x2 arithmetic.
+// persistent CTAs, cp.async pipeline, two elements per thread in packed f32x2
+// arithmetic.
 //
 // Same mathematics, plan and summation order as the modal path of assemble.cu (the
 // 2x2x2 Gauss sum evaluated exactly in the monomial basis of grad u through an
 // 8-point Walsh-Hadamard transform); what changes is the schedule:
-//   * each CTA walks its blocks b = blockIdx.x, blockIdx.x + gridDim.x, ...; while
-//     block b is computed, the coordinates and the input vector of the next block
-//     are gathered into the other shared-memory buffer with cp.async (4-byte
-//     copies, one per value), and the node ids / partial slots of the block after
-//     that are already in registers -- the HBM latency of the gathers is hidden
-//     behind compute;
-//   * every thread evaluates two elements at once, one per lane of f32x2 registers,
-//     so each arithmetic instruction serves two elements;
+//   * each CTA walks its blocks b_0 = blockIdx.x, b_1 = b_0 + gridDim.x, ...; while
+//     block b_i is computed, the coordinates and input vector of b_{i+1} are gathered
+//     into the other shared-memory buffer (4-byte cp.async per value) and the node
+//     ids of b_{i+2} are copied into a two-entry shared ring; the connectivity of
+//     b_{i+1} is loaded into registers at the end of b_i's compute -- no global
+//     load sits between a block's barrier and its arithmetic;
+//   * every thread evaluates two elements at once, one per lane of f32x2 registers;
 //   * element results stay in registers until the colour-ordered shared-memory
-//     accumulation (one barrier per colour), as in the scalar kernel.
+//     accumulation (one barrier per colour), as in the scalar kernel;
+//   * DIAG instantiation: blocks whose elements are axis-aligned boxes (verified on
+//     the host in FP32 and FP64) have a diagonal Jacobian, and the monomial terms
+//     reduce to per-component products.
 #include "tg_common.cuh"
 #include "tg_f32x2.cuh"
 #include "tg_internal.h"
 
 namespace tg {
 
-constexpr int P5_THREADS = 128;
-constexpr int P5_NPT = 6;  // staged nodes per thread per block
-constexpr int P5_MAX_LOCAL = P5_THREADS * P5_NPT;
+constexpr int P6_THREADS = 128;
+constexpr int P6_NPT = 6;  // staged nodes per thread per block
+constexpr int P6_EPT = 4;  // element positions per thread per block
+constexpr int P6_MAX_LOCAL = P6_THREADS * P6_NPT;
+constexpr int P6_MAX_ELEMS = P6_THREADS * P6_EPT;
 
-__device__ __forceinline__ int swz5(int l) { return l ^ ((l >> 3) & 7); }
-__device__ __forceinline__ int hex_t5(int a) {
+__device__ __forceinline__ int hex_t6(int a) {
   return (a == 2) ? 3 : (a == 3) ? 2 : (a == 6) ? 7 : (a == 7) ? 6 : a;
 }
 
@@ -37,8 +40,8 @@ __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gsrc) {
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
-__device__ __forceinline__ void cp_async_wait1() {
-  asm volatile("cp.async.wait_group 1;" ::: "memory");
+__device__ __forceinline__ void cp_async_wait0() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 __device__ __forceinline__ void had8(f2 (&m)[8]) {
@@ -68,7 +71,7 @@ __device__ __forceinline__ f2 dot3c(const f2 (&g)[3], const f2 (&R)[3][3], int c
   return fma2(g[2], R[2][c], fma2(g[1], R[1][c], g[0] * R[0][c]));
 }
 
-// two-direction monomial (directions P < Q), see le_two_dir in assemble.cu
+// two-direction monomial (directions P < Q), general Jacobian (see le_two_dir)
 template <int P, int Q>
 __device__ __forceinline__ void le_two_dir2(const f2 (&R)[3][3], const f2 (&Gm)[3][3],
                                             const f2 (&gp)[3], const f2 (&gq)[3], f2 mu, f2 lam,
@@ -85,21 +88,50 @@ __device__ __forceinline__ void le_two_dir2(const f2 (&R)[3][3], const f2 (&Gm)[
   }
 }
 
-// M: transformed nodal values (component j, monomial S); out: dE/dM_S (unscaled
-// transform coefficients) for linear elasticity on a parallelepiped with
-// R = inv(8 J) and detJm = det(8 J).
+// two-direction monomial with R = diag(r): the metric is diag(r^2) and R[j][P] = 0
+// unless j == P
+template <int P, int Q>
+__device__ __forceinline__ void le_two_dir2_diag(const f2 (&r)[3], const f2 (&rr)[3],
+                                                 const f2 (&gp)[3], const f2 (&gq)[3], f2 mu,
+                                                 f2 lam, f2 (&Fp)[3], f2 (&Fq)[3]) {
+  const f2 a_pp = gp[P] * r[P], a_pq = gp[Q] * r[Q];
+  const f2 a_qp = gq[P] * r[P], a_qq = gq[Q] * r[Q];
+  const f2 lt = lam * (a_pp + a_qq);
+  const f2 c1 = mu * rr[P], d2 = mu * rr[Q];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    Fp[j] = c1 * gp[j];
+    Fq[j] = d2 * gq[j];
+  }
+  Fp[P] = fma2(fma2(mu, a_pp, lt), r[P], Fp[P]);
+  Fp[Q] = fma2(mu * a_qp, r[Q], Fp[Q]);
+  Fq[P] = fma2(mu * a_pq, r[P], Fq[P]);
+  Fq[Q] = fma2(fma2(mu, a_qq, lt), r[Q], Fq[Q]);
+}
+
+// M: transformed nodal values (component j, monomial S); out: dE/dM_S for linear
+// elasticity on a parallelepiped with R = inv(8 J), detJm = det(8 J).  DIAG: only
+// the diagonal of R is read.
+template <bool DIAG>
 __device__ __forceinline__ void le_modal_pair(const f2 (&R)[3][3], f2 detJm, f2 mu, f2 lam,
                                               const f2 (&M)[3][8], f2 (&dM)[3][8]) {
   const float g2f = float(HEX_GAUSS) * float(HEX_GAUSS);
   const f2 s0 = detJm * f2_bcast(1.0f / 64);
   const f2 s1 = s0 * f2_bcast(g2f);
   const f2 s2 = s1 * f2_bcast(g2f);
+  const f2 r[3] = {R[0][0], R[1][1], R[2][2]};
   {  // constant monomial: directions (x, y, z) carry (M1, M2, M4)
     f2 H[3][3];
 #pragma unroll
     for (int j = 0; j < 3; ++j)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) H[j][k] = fma2(R[k][2], M[j][4], fma2(R[k][1], M[j][2], R[k][0] * M[j][1]));
+      for (int k = 0; k < 3; ++k) {
+        if constexpr (DIAG) {
+          H[j][k] = r[k] * M[j][1 << k];
+        } else {
+          H[j][k] = fma2(R[k][2], M[j][4], fma2(R[k][1], M[j][2], R[k][0] * M[j][1]));
+        }
+      }
     const f2 m0 = mu * s0;
     const f2 lt = (lam * s0) * (H[0][0] + H[1][1] + H[2][2]);
     f2 P[3][3];
@@ -115,19 +147,17 @@ __device__ __forceinline__ void le_modal_pair(const f2 (&R)[3][3], f2 detJm, f2 
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       dM[j][0] = f2_zero();
-      dM[j][1] = fma2(P[j][2], R[2][0], fma2(P[j][1], R[1][0], P[j][0] * R[0][0]));
-      dM[j][2] = fma2(P[j][2], R[2][1], fma2(P[j][1], R[1][1], P[j][0] * R[0][1]));
-      dM[j][4] = fma2(P[j][2], R[2][2], fma2(P[j][1], R[1][2], P[j][0] * R[0][2]));
+      if constexpr (DIAG) {
+        dM[j][1] = P[j][0] * r[0];
+        dM[j][2] = P[j][1] * r[1];
+        dM[j][4] = P[j][2] * r[2];
+      } else {
+        dM[j][1] = fma2(P[j][2], R[2][0], fma2(P[j][1], R[1][0], P[j][0] * R[0][0]));
+        dM[j][2] = fma2(P[j][2], R[2][1], fma2(P[j][1], R[1][1], P[j][0] * R[0][1]));
+        dM[j][4] = fma2(P[j][2], R[2][2], fma2(P[j][1], R[1][2], P[j][0] * R[0][2]));
+      }
     }
   }
-  f2 Gm[3][3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int b = a; b < 3; ++b) {
-      Gm[a][b] = fma2(R[2][a], R[2][b], fma2(R[1][a], R[1][b], R[0][a] * R[0][b]));
-      Gm[b][a] = Gm[a][b];
-    }
   const f2 mu1 = mu * s1, lam1 = lam * s1;
   f2 g12[3], g13[3], g23[3], g123[3], Fp[3], Fq[3];
 #pragma unroll
@@ -137,26 +167,51 @@ __device__ __forceinline__ void le_modal_pair(const f2 (&R)[3][3], f2 detJm, f2 
     g23[j] = M[j][6];
     g123[j] = M[j][7];
   }
-  le_two_dir2<1, 2>(R, Gm, g12, g13, mu1, lam1, Fp, Fq);  // monomial x
-#pragma unroll
-  for (int j = 0; j < 3; ++j) { dM[j][3] = Fp[j]; dM[j][5] = Fq[j]; }
-  le_two_dir2<0, 2>(R, Gm, g12, g23, mu1, lam1, Fp, Fq);  // monomial y
-#pragma unroll
-  for (int j = 0; j < 3; ++j) { dM[j][3] = dM[j][3] + Fp[j]; dM[j][6] = Fq[j]; }
-  le_two_dir2<0, 1>(R, Gm, g13, g23, mu1, lam1, Fp, Fq);  // monomial z
-#pragma unroll
-  for (int j = 0; j < 3; ++j) { dM[j][5] = dM[j][5] + Fp[j]; dM[j][6] = dM[j][6] + Fq[j]; }
-  // monomials yz, xz, xy: mu tr(Gm) g + (mu + lam) R R^T g, g = M123
   const f2 mu2 = mu * s2, ml2 = (mu + lam) * s2;
-  const f2 trG = Gm[0][0] + Gm[1][1] + Gm[2][2];
-  f2 h[3];
+  if constexpr (DIAG) {
+    const f2 rr[3] = {r[0] * r[0], r[1] * r[1], r[2] * r[2]};
+    le_two_dir2_diag<1, 2>(r, rr, g12, g13, mu1, lam1, Fp, Fq);  // monomial x
 #pragma unroll
-  for (int i = 0; i < 3; ++i) h[i] = dot3c(g123, R, i);
-  const f2 a = mu2 * trG;
+    for (int j = 0; j < 3; ++j) { dM[j][3] = Fp[j]; dM[j][5] = Fq[j]; }
+    le_two_dir2_diag<0, 2>(r, rr, g12, g23, mu1, lam1, Fp, Fq);  // monomial y
 #pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const f2 rh = fma2(R[j][2], h[2], fma2(R[j][1], h[1], R[j][0] * h[0]));
-    dM[j][7] = fma2(ml2, rh, a * g123[j]);
+    for (int j = 0; j < 3; ++j) { dM[j][3] = dM[j][3] + Fp[j]; dM[j][6] = Fq[j]; }
+    le_two_dir2_diag<0, 1>(r, rr, g13, g23, mu1, lam1, Fp, Fq);  // monomial z
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { dM[j][5] = dM[j][5] + Fp[j]; dM[j][6] = dM[j][6] + Fq[j]; }
+    // yz, xz, xy: (mu tr(Gm) + (mu + lam) r_j^2) g_j
+    const f2 a = mu2 * (rr[0] + rr[1] + rr[2]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dM[j][7] = fma2(ml2, rr[j], a) * g123[j];
+  } else {
+    f2 Gm[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = a; b < 3; ++b) {
+        Gm[a][b] = fma2(R[2][a], R[2][b], fma2(R[1][a], R[1][b], R[0][a] * R[0][b]));
+        Gm[b][a] = Gm[a][b];
+      }
+    le_two_dir2<1, 2>(R, Gm, g12, g13, mu1, lam1, Fp, Fq);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { dM[j][3] = Fp[j]; dM[j][5] = Fq[j]; }
+    le_two_dir2<0, 2>(R, Gm, g12, g23, mu1, lam1, Fp, Fq);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { dM[j][3] = dM[j][3] + Fp[j]; dM[j][6] = Fq[j]; }
+    le_two_dir2<0, 1>(R, Gm, g13, g23, mu1, lam1, Fp, Fq);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { dM[j][5] = dM[j][5] + Fp[j]; dM[j][6] = dM[j][6] + Fq[j]; }
+    // yz, xz, xy: mu tr(Gm) g + (mu + lam) R R^T g, g = M123
+    const f2 trG = Gm[0][0] + Gm[1][1] + Gm[2][2];
+    f2 h[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) h[i] = dot3c(g123, R, i);
+    const f2 a = mu2 * trG;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const f2 rh = fma2(R[j][2], h[2], fma2(R[j][1], h[1], R[j][0] * h[0]));
+      dM[j][7] = fma2(ml2, rh, a * g123[j]);
+    }
   }
 }
 
@@ -180,150 +235,197 @@ __device__ __forceinline__ f2 inv3_pair(const f2 (&J)[3][3], f2 (&Ji)[3][3]) {
   return det;
 }
 
-// shared-memory layout (floats), nl8 = node slots (multiple of 8):
-//   buffer s (s = 0, 1) at s * 10 nl8: X (4 nl8) | W (4 nl8) | GID (nl8) | SLOT (nl8)
-//   Y at 20 nl8 (4 nl8)
-template <int MODE>
-__global__ void __launch_bounds__(P5_THREADS, 3)
-    hex_le_f32x2_kernel(const tg_block_plan p, int n_blocks, const float* __restrict__ coords,
-                        const float* __restrict__ fin, const uint8_t* __restrict__ fixed,
-                        const float* __restrict__ vin, float* __restrict__ y,
-                        float* __restrict__ partials, float mu_s, float lam_s, int nl8) {
+__device__ __forceinline__ void unpack_lconn(uint4 v, int (&l)[8]) {
+  l[0] = v.x & 0xffff; l[1] = v.x >> 16; l[2] = v.y & 0xffff; l[3] = v.y >> 16;
+  l[4] = v.z & 0xffff; l[5] = v.z >> 16; l[6] = v.w & 0xffff; l[7] = v.w >> 16;
+}
+
+// shared-memory layout (32-bit words), nl8 = node slots (multiple of 8):
+//   data buffer s (s = 0, 1) at s * 8 nl8: X (4 nl8) | W (4 nl8)
+//   node-id ring r (r = 0, 1) at 16 nl8 + r nl8, slot ring r at 18 nl8 + r nl8
+//   Y at 20 nl8 (4 nl8)                                            total 24 nl8
+template <int MODE, bool DIAG>
+__global__ void __launch_bounds__(P6_THREADS, 3)
+    hex_le_f32x2_kernel(const tg_block_plan p, int b_begin, int b_end,
+                        const float* __restrict__ coords, const float* __restrict__ fin,
+                        const uint8_t* __restrict__ fixed, const float* __restrict__ vin,
+                        float* __restrict__ y, float* __restrict__ partials, float mu_s,
+                        float lam_s, int nl8) {
   extern __shared__ __align__(16) float sm[];
+  int* const ring = reinterpret_cast<int*>(sm + 16 * nl8);
+  int* const qring = reinterpret_cast<int*>(sm + 18 * nl8);
   float* const Ybuf = sm + 20 * nl8;
   const int tid = threadIdx.x;
-  constexpr int NT = P5_THREADS;
+  constexpr int NT = P6_THREADS;
+  const int nblk = b_end - b_begin;
+  const int stride = gridDim.x;
 
   for (int l = tid; l < nl8; l += NT) {
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      sm[s * 10 * nl8 + l * 4 + 3] = 0.f;
-      sm[s * 10 * nl8 + 4 * nl8 + l * 4 + 3] = 0.f;
+      sm[s * 8 * nl8 + l * 4 + 3] = 0.f;
+      sm[s * 8 * nl8 + 4 * nl8 + l * 4 + 3] = 0.f;
     }
     reinterpret_cast<float4*>(Ybuf)[l] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 
-  int G1[P5_NPT], S1[P5_NPT], G2[P5_NPT], S2[P5_NPT];
-  auto load_gs = [&](int b, int (&G)[P5_NPT], int (&S)[P5_NPT]) {
-    const int n0 = p.blk_node_ptr[b], nl = p.blk_node_ptr[b + 1] - n0;
+  // copy the node ids and shared-memory slots of block b into ring entry r (each
+  // thread its own entries)
+  auto issue_ids = [&](int b, int r) {
+    const int n0 = __ldg(p.blk_node_ptr + b), nl = __ldg(p.blk_node_ptr + b + 1) - n0;
 #pragma unroll
-    for (int k = 0; k < P5_NPT; ++k) {
-      const int l = tid + k * NT;
-      G[k] = (l < nl) ? __ldg(p.lnode_gid + n0 + l) : 0;
-      S[k] = (l < nl) ? __ldg(p.lnode_slot + n0 + l) : 0;
-    }
-  };
-  auto issue = [&](int b, int s, const int (&G)[P5_NPT], const int (&S)[P5_NPT]) {
-    float* X = sm + s * 10 * nl8;
-    float* W = X + 4 * nl8;
-    int* GID = reinterpret_cast<int*>(X + 8 * nl8);
-    int* SLOT = GID + nl8;
-    const int nl = p.blk_node_ptr[b + 1] - p.blk_node_ptr[b];
-#pragma unroll
-    for (int k = 0; k < P5_NPT; ++k) {
+    for (int k = 0; k < P6_NPT; ++k) {
       const int l = tid + k * NT;
       if (l < nl) {
-        const int q = swz5(l);
-        const int64_t g = G[k];
+        cp_async4(ring + r * nl8 + l, p.lnode_gid + n0 + l);
+        cp_async4(qring + r * nl8 + l, p.lnode_smem + n0 + l);
+      }
+    }
+  };
+  // gather coordinates and input values of block b (ids in ring slot r) into buffer s
+  auto issue_data = [&](int b, int r, int s) {
+    float* X = sm + s * 8 * nl8;
+    float* W = X + 4 * nl8;
+    const int nl = __ldg(p.blk_node_ptr + b + 1) - __ldg(p.blk_node_ptr + b);
+#pragma unroll
+    for (int k = 0; k < P6_NPT; ++k) {
+      const int l = tid + k * NT;
+      if (l < nl) {
+        const int q = qring[r * nl8 + l];
+        const int64_t g = ring[r * nl8 + l];
 #pragma unroll
         for (int d = 0; d < 3; ++d) cp_async4(X + q * 4 + d, coords + g * 3 + d);
 #pragma unroll
         for (int d = 0; d < 3; ++d) cp_async4(W + q * 4 + d, fin + g * 3 + d);
-        GID[l] = G[k];
-        SLOT[l] = S[k];
       }
     }
   };
+  auto load_lconn4 = [&](int b, uint4 (&LC)[P6_EPT]) {
+    const int e0 = __ldg(p.blk_elem_ptr + b), ne = __ldg(p.blk_elem_ptr + b + 1) - e0;
+#pragma unroll
+    for (int j = 0; j < P6_EPT; ++j) {
+      const int k = tid + j * NT;
+      LC[j] = (k < ne) ? __ldg(reinterpret_cast<const uint4*>(p.lconn) + e0 + k)
+                       : make_uint4(0, 0, 0, 0);
+    }
+  };
 
-  const int stride = gridDim.x;
-  int b = blockIdx.x;
-  if (b < n_blocks) {
-    load_gs(b, G1, S1);
-    issue(b, 0, G1, S1);
-  }
+  // prologue: ids of the first block, then its data and the ids of the second
+  int bi = blockIdx.x;
+  if (bi < nblk) issue_ids(b_begin + bi, 0);
   cp_async_commit();
-  if (b + stride < n_blocks) load_gs(b + stride, G1, S1);
+  cp_async_wait0();
+  __syncthreads();
+  if (bi < nblk) issue_data(b_begin + bi, 0, 0);
+  if (bi + stride < nblk) issue_ids(b_begin + bi + stride, 1);
+  cp_async_commit();
+  uint4 LC[P6_EPT];
+  if (bi < nblk) load_lconn4(b_begin + bi, LC);
 
   const f2 mu = f2_bcast(mu_s), lam = f2_bcast(lam_s);
-  for (int it = 0; b < n_blocks; ++it, b += stride) {
+  for (int it = 0; bi < nblk; ++it, bi += stride) {
+    const int b = b_begin + bi;
     const int s = it & 1;
-    if (b + stride < n_blocks) issue(b + stride, s ^ 1, G1, S1);
-    cp_async_commit();
-    if (b + 2 * stride < n_blocks) load_gs(b + 2 * stride, G2, S2);
-    cp_async_wait1();
-    __syncthreads();
-
-    const float* X = sm + s * 10 * nl8;
-    float* W = const_cast<float*>(X) + 4 * nl8;
-    const int* GID = reinterpret_cast<const int*>(X + 8 * nl8);
-    const int* SLOT = GID + nl8;
-    const int nl = p.blk_node_ptr[b + 1] - p.blk_node_ptr[b];
-    if (MODE == TG_MODE_HVP && fixed) {
-      for (int l = tid; l < nl; l += NT) {
-        const int64_t g = GID[l];
+    cp_async_wait0();
+    __syncthreads();  // data of b in buffer s, ids of the next block in ring slot s ^ 1
+    const int n0 = __ldg(p.blk_node_ptr + b);
+    const int nl = __ldg(p.blk_node_ptr + b + 1) - n0;
+    int Gwb[P6_NPT], Swb[P6_NPT], Qwb[P6_NPT];
 #pragma unroll
-        for (int d = 0; d < 3; ++d)
-          if (fixed[g * 3 + d]) W[swz5(l) * 4 + d] = 0.f;
+    for (int k = 0; k < P6_NPT; ++k) {
+      const int l = tid + k * NT;
+      Gwb[k] = (l < nl) ? ring[s * nl8 + l] : 0;
+      Qwb[k] = (l < nl) ? qring[s * nl8 + l] : 0;
+      Swb[k] = (l < nl) ? __ldg(p.lnode_slot + n0 + l) : 0;
+    }
+    if (bi + stride < nblk) issue_data(b + stride, s ^ 1, s ^ 1);
+    if (bi + 2 * stride < nblk) issue_ids(b + 2 * stride, s);
+    cp_async_commit();
+
+    const float* X = sm + s * 8 * nl8;
+    float* W = const_cast<float*>(X) + 4 * nl8;
+    if (MODE == TG_MODE_HVP && fixed) {
+#pragma unroll
+      for (int k = 0; k < P6_NPT; ++k) {
+        const int l = tid + k * NT;
+        if (l < nl) {
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            if (fixed[(int64_t)Gwb[k] * 3 + d]) W[Qwb[k] * 4 + d] = 0.f;
+        }
       }
       __syncthreads();
     }
 
-    const int e_base = p.blk_elem_ptr[b];
-    const int ne = p.blk_elem_ptr[b + 1] - e_base;
-    const int c_begin = p.blk_color_ptr[b];
-    const int c_last = p.blk_color_ptr[b + 1] - 1;
-    for (int k0 = 0; k0 < ne; k0 += 2 * NT) {
+    const int ne = __ldg(p.blk_elem_ptr + b + 1) - __ldg(p.blk_elem_ptr + b);
+    const int c_begin = __ldg(p.blk_color_ptr + b);
+    const int c_last = __ldg(p.blk_color_ptr + b + 1) - 1;
+#pragma unroll
+    for (int ch = 0; ch < P6_EPT / 2; ++ch) {
+      const int k0 = ch * 2 * NT;
+      if (k0 >= ne) break;  // uniform
       const int kA = k0 + tid, kB = k0 + NT + tid;
       const bool actA = kA < ne, actB = kB < ne;
       float YA[8][3], YB[8][3];
       int qA[8], qB[8];
+      unpack_lconn(LC[2 * ch], qA);
+      unpack_lconn(actB ? LC[2 * ch + 1] : LC[2 * ch], qB);
       if (actA) {
-        int lcA[8], lcB[8];
-        load_lconn<8>(p.lconn + (int64_t)(e_base + kA) * 8, lcA);
-        load_lconn<8>(p.lconn + (int64_t)(e_base + (actB ? kB : kA)) * 8, lcB);
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          qA[a] = swz5(lcA[a]);
-          qB[a] = swz5(lcB[a]);
-        }
-        f2 Jm[3][3], R[3][3];
+        f2 R[3][3], detJm;
         {
           const float4 a0 = reinterpret_cast<const float4*>(X)[qA[0]];
           const float4 b0 = reinterpret_cast<const float4*>(X)[qB[0]];
-          const int ed[3] = {1, 3, 4};
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            const float4 ai = reinterpret_cast<const float4*>(X)[qA[ed[i]]];
-            const float4 bi = reinterpret_cast<const float4*>(X)[qB[ed[i]]];
-            Jm[i][0] = f2_make(4.f * (ai.x - a0.x), 4.f * (bi.x - b0.x));
-            Jm[i][1] = f2_make(4.f * (ai.y - a0.y), 4.f * (bi.y - b0.y));
-            Jm[i][2] = f2_make(4.f * (ai.z - a0.z), 4.f * (bi.z - b0.z));
+          const float4 a1 = reinterpret_cast<const float4*>(X)[qA[1]];
+          const float4 b1 = reinterpret_cast<const float4*>(X)[qB[1]];
+          const float4 a3 = reinterpret_cast<const float4*>(X)[qA[3]];
+          const float4 b3 = reinterpret_cast<const float4*>(X)[qB[3]];
+          const float4 a4 = reinterpret_cast<const float4*>(X)[qA[4]];
+          const float4 b4 = reinterpret_cast<const float4*>(X)[qB[4]];
+          if constexpr (DIAG) {
+            const float jA0 = 4.f * (a1.x - a0.x), jB0 = 4.f * (b1.x - b0.x);
+            const float jA1 = 4.f * (a3.y - a0.y), jB1 = 4.f * (b3.y - b0.y);
+            const float jA2 = 4.f * (a4.z - a0.z), jB2 = 4.f * (b4.z - b0.z);
+            R[0][0] = f2_make(__frcp_rn(jA0), __frcp_rn(jB0));
+            R[1][1] = f2_make(__frcp_rn(jA1), __frcp_rn(jB1));
+            R[2][2] = f2_make(__frcp_rn(jA2), __frcp_rn(jB2));
+            detJm = f2_make(jA0 * jA1 * jA2, jB0 * jB1 * jB2);
+          } else {
+            f2 Jm[3][3];
+            Jm[0][0] = f2_make(4.f * (a1.x - a0.x), 4.f * (b1.x - b0.x));
+            Jm[0][1] = f2_make(4.f * (a1.y - a0.y), 4.f * (b1.y - b0.y));
+            Jm[0][2] = f2_make(4.f * (a1.z - a0.z), 4.f * (b1.z - b0.z));
+            Jm[1][0] = f2_make(4.f * (a3.x - a0.x), 4.f * (b3.x - b0.x));
+            Jm[1][1] = f2_make(4.f * (a3.y - a0.y), 4.f * (b3.y - b0.y));
+            Jm[1][2] = f2_make(4.f * (a3.z - a0.z), 4.f * (b3.z - b0.z));
+            Jm[2][0] = f2_make(4.f * (a4.x - a0.x), 4.f * (b4.x - b0.x));
+            Jm[2][1] = f2_make(4.f * (a4.y - a0.y), 4.f * (b4.y - b0.y));
+            Jm[2][2] = f2_make(4.f * (a4.z - a0.z), 4.f * (b4.z - b0.z));
+            detJm = inv3_pair(Jm, R);
           }
         }
-        const f2 detJm = inv3_pair(Jm, R);
         f2 M[3][8];
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
           const float4 wa = reinterpret_cast<const float4*>(W)[qA[a]];
           const float4 wb = reinterpret_cast<const float4*>(W)[qB[a]];
-          M[0][hex_t5(a)] = f2_make(wa.x, wb.x);
-          M[1][hex_t5(a)] = f2_make(wa.y, wb.y);
-          M[2][hex_t5(a)] = f2_make(wa.z, wb.z);
+          M[0][hex_t6(a)] = f2_make(wa.x, wb.x);
+          M[1][hex_t6(a)] = f2_make(wa.y, wb.y);
+          M[2][hex_t6(a)] = f2_make(wa.z, wb.z);
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j) had8(M[j]);
         f2 dM[3][8];
-        le_modal_pair(R, detJm, mu, lam, M, dM);
+        le_modal_pair<DIAG>(R, detJm, mu, lam, M, dM);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           had8t(dM[j]);
 #pragma unroll
-          for (int a = 0; a < 8; ++a) f2_split(dM[j][hex_t5(a)], YA[a][j], YB[a][j]);
+          for (int a = 0; a < 8; ++a) f2_split(dM[j][hex_t6(a)], YA[a][j], YB[a][j]);
         }
       }
       for (int c = c_begin; c < c_last; ++c) {
-        const int lo = max(p.color_ofs[c], k0);
-        const int hi = min(p.color_ofs[c + 1], k0 + 2 * NT);
+        const int lo = max(__ldg(p.color_ofs + c), k0);
+        const int hi = min(__ldg(p.color_ofs + c + 1), k0 + 2 * NT);
         if (lo >= hi) continue;  // uniform over the block
         if (actA && kA >= lo && kA < hi) {
 #pragma unroll
@@ -344,17 +446,19 @@ __global__ void __launch_bounds__(P5_THREADS, 3)
         __syncthreads();
       }
     }
+    if (bi + stride < nblk) load_lconn4(b + stride, LC);
 
     // write back this block and clear the accumulator
-    for (int l = tid; l < nl; l += NT) {
-      const int q = swz5(l);
-      float4* yp = reinterpret_cast<float4*>(Ybuf) + q;
+#pragma unroll
+    for (int k = 0; k < P6_NPT; ++k) {
+      const int l = tid + k * NT;
+      if (l >= nl) continue;
+      float4* yp = reinterpret_cast<float4*>(Ybuf) + Qwb[k];
       const float4 yv = *yp;
       *yp = make_float4(0.f, 0.f, 0.f, 0.f);
-      const int64_t g = GID[l];
-      const int slot = SLOT[l];
+      const int64_t g = Gwb[k];
       const float vals[3] = {yv.x, yv.y, yv.z};
-      if (slot < 0) {
+      if (Swb[k] < 0) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const int64_t dof = g * 3 + d;
@@ -364,51 +468,58 @@ __global__ void __launch_bounds__(P5_THREADS, 3)
         }
       } else {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) partials[(int64_t)slot * 3 + d] = vals[d];
+        for (int d = 0; d < 3; ++d) partials[(int64_t)Swb[k] * 3 + d] = vals[d];
       }
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < P5_NPT; ++k) {
-      G1[k] = G2[k];
-      S1[k] = S2[k];
-    }
   }
-  asm volatile("cp.async.wait_all;" ::: "memory");
+  cp_async_wait0();
+}
+
+template <int MODE, bool DIAG>
+static int launch6(const tg_block_plan* plan, int b0, int b1, const float* coords,
+                   const float* fin, const uint8_t* fixed, const float* vin, float* y,
+                   float* partials, float mu, float lam, int nl8, size_t smem, int sms,
+                   cudaStream_t st) {
+  if (b1 <= b0) return TG_OK;
+  auto k = hex_le_f32x2_kernel<MODE, DIAG>;
+  TG_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "hex f32x2: shared memory attribute"));
+  int per_sm = 0;
+  TG_TRY(cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P6_THREADS, smem),
+                    "hex f32x2: occupancy"));
+  const int grid = std::max(1, std::min(b1 - b0, sms * std::max(per_sm, 1)));
+  k<<<grid, P6_THREADS, smem, st>>>(*plan, b0, b1, coords, fin, fixed, vin, y, partials, mu, lam,
+                                    nl8);
+  return launch_check("hex f32x2 kernel");
 }
 
 int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords, const float* u,
                         const float* v, const uint8_t* fixed, float* y, float* partials,
                         float mu, float lam, cudaStream_t st) {
-  const int n_aff = plan->n_affine_blocks;
+  const int n_aff = plan->n_affine_blocks, n_diag = plan->n_diag_blocks;
   if (n_aff <= 0) return TG_OK;
-  if (plan->max_local_nodes > P5_MAX_LOCAL) return TG_ERR_UNSUPPORTED;
+  if (plan->max_local_nodes > P6_MAX_LOCAL || plan->max_block_elems > P6_MAX_ELEMS)
+    return TG_ERR_UNSUPPORTED;
+  if (n_diag < 0 || n_diag > n_aff) return set_error(TG_ERR_VALUE, "plan.n_diag_blocks out of range");
   const int nl8 = (plan->max_local_nodes + 7) & ~7;
   const size_t smem = (size_t)24 * nl8 * sizeof(float);
-  int dev = 0, sms = 0, per_sm = 0, optin = 0;
+  int dev = 0, sms = 0, optin = 0;
   TG_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
   TG_TRY(cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
   TG_TRY(cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
                     "shared memory limit"));
   if (smem > (size_t)optin) return TG_ERR_UNSUPPORTED;
   if (mode == TG_MODE_HVP) {
-    auto k = hex_le_f32x2_kernel<TG_MODE_HVP>;
-    TG_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "hex f32x2: shared memory attribute"));
-    TG_TRY(cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P5_THREADS, smem),
-                      "hex f32x2: occupancy"));
-    const int grid = std::max(1, std::min(n_aff, sms * std::max(per_sm, 1)));
-    k<<<grid, P5_THREADS, smem, st>>>(*plan, n_aff, coords, v, fixed, v, y, partials, mu, lam, nl8);
-  } else {
-    auto k = hex_le_f32x2_kernel<TG_MODE_RESIDUAL>;
-    TG_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "hex f32x2: shared memory attribute"));
-    TG_TRY(cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P5_THREADS, smem),
-                      "hex f32x2: occupancy"));
-    const int grid = std::max(1, std::min(n_aff, sms * std::max(per_sm, 1)));
-    k<<<grid, P5_THREADS, smem, st>>>(*plan, n_aff, coords, u, fixed, v, y, partials, mu, lam, nl8);
+    TG_TRY((launch6<TG_MODE_HVP, true>(plan, 0, n_diag, coords, v, fixed, v, y, partials, mu, lam,
+                                       nl8, smem, sms, st)));
+    return launch6<TG_MODE_HVP, false>(plan, n_diag, n_aff, coords, v, fixed, v, y, partials, mu,
+                                       lam, nl8, smem, sms, st);
   }
-  return launch_check("hex f32x2 kernel");
+  TG_TRY((launch6<TG_MODE_RESIDUAL, true>(plan, 0, n_diag, coords, u, fixed, v, y, partials, mu,
+                                          lam, nl8, smem, sms, st)));
+  return launch6<TG_MODE_RESIDUAL, false>(plan, n_diag, n_aff, coords, u, fixed, v, y, partials,
+                                          mu, lam, nl8, smem, sms, st);
 }
 
 }  // namespace tg

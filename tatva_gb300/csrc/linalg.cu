@@ -19,10 +19,40 @@
 
 namespace tg {
 
-constexpr int DOT_CHUNKS = 1024;
+constexpr int DOT_CHUNKS = 2048;
 constexpr int DOT_THREADS = 256;
 constexpr int SCAL_RZ = 0, SCAL_PQ = 1, SCAL_ALPHA = 2, SCAL_BETA = 3, SCAL_RR = 4,
               SCAL_FLAG = 6, SCAL_N = 8;
+
+// ------------------------------------------------------------------ dot accumulators
+// FP32 vectors: each thread accumulates x_i y_i as an unevaluated pair (hi, lo) of
+// floats -- the product is split exactly with an FMA and added with a two-sum, so the
+// thread's partial keeps about 48 bits -- and only the per-thread partials enter the
+// FP64 tree reduction.  (This GPU's FP64 rate is a small fraction of FP32: per-element
+// FP64 conversions and multiply-adds made the dots several times slower than their
+// memory traffic.)  FP64 vectors accumulate in FP64.
+template <class T>
+struct DotAcc;
+template <>
+struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float pr = a * b;
+    const float pe = fmaf(a, b, -pr);
+    const float s = hi + pr;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (pr - bp);
+    hi = s;
+    lo += err + pe;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+template <>
+struct DotAcc<double> {
+  double v = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { v += a * b; }
+  __device__ __forceinline__ double value() const { return v; }
+};
 
 // ------------------------------------------------------------------ reductions
 template <int K>
@@ -44,10 +74,29 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[K], double* __res
   }
 }
 
+// fixed partition into DOT_CHUNKS chunks whose starts are multiples of 4 elements
 __device__ __forceinline__ void chunk_range(int64_t n, int64_t& i0, int64_t& i1) {
-  const int64_t chunk = (n + DOT_CHUNKS - 1) / DOT_CHUNKS;
-  i0 = (int64_t)blockIdx.x * chunk;
+  const int64_t chunk = (((n + DOT_CHUNKS - 1) / DOT_CHUNKS) + 3) & ~int64_t(3);
+  i0 = min(n, (int64_t)blockIdx.x * chunk);
   i1 = min(n, i0 + chunk);
+}
+
+// 16-byte vector access of 4 consecutive values (4-aligned index, 16-byte aligned base)
+__device__ __forceinline__ void ldv(const float* p, float (&v)[4]) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ldv(const double* p, double (&v)[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0];
+  const double2 b = reinterpret_cast<const double2*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void stv(float* p, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void stv(double* p, const double (&v)[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
 template <class T>
@@ -56,8 +105,17 @@ __global__ void __launch_bounds__(DOT_THREADS)
                        double* __restrict__ part) {
   int64_t i0, i1;
   chunk_range(n, i0, i1);
-  double v[1] = {0.0};
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) v[0] += (double)x[i] * (double)y[i];
+  const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
+  DotAcc<T> acc;
+  for (int64_t i = i0 + 4 * threadIdx.x; i < iv; i += 4 * DOT_THREADS) {
+    T a[4], b[4];
+    ldv(x + i, a);
+    ldv(y + i, b);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc.add(a[k], b[k]);
+  }
+  for (int64_t i = iv + threadIdx.x; i < i1; i += DOT_THREADS) acc.add(x[i], y[i]);
+  double v[1] = {acc.value()};
   block_reduce_store<1>(v, part + blockIdx.x);
 }
 
@@ -139,15 +197,30 @@ __global__ void __launch_bounds__(DOT_THREADS)
                    T* __restrict__ z, T* __restrict__ p, double* __restrict__ part) {
   int64_t i0, i1;
   chunk_range(n, i0, i1);
-  double v[2] = {0.0, 0.0};
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) {
+  const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
+  DotAcc<T> a0, a1;
+  for (int64_t i = i0 + 4 * threadIdx.x; i < iv; i += 4 * DOT_THREADS) {
+    T rr[4], dd[4], zz[4];
+    ldv(r + i, rr);
+    ldv(diag + i, dd);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      zz[k] = rr[k] / dd[k];
+      a0.add(rr[k], zz[k]);
+      a1.add(rr[k], rr[k]);
+    }
+    stv(z + i, zz);
+    stv(p + i, zz);
+  }
+  for (int64_t i = iv + threadIdx.x; i < i1; i += DOT_THREADS) {
     const T ri = r[i];
     const T zi = ri / diag[i];
     z[i] = zi;
     p[i] = zi;
-    v[0] += (double)ri * (double)zi;
-    v[1] += (double)ri * (double)ri;
+    a0.add(ri, zi);
+    a1.add(ri, ri);
   }
+  double v[2] = {a0.value(), a1.value()};
   block_reduce_store<2>(v, part + 2 * blockIdx.x);
 }
 
@@ -193,17 +266,38 @@ __global__ void __launch_bounds__(DOT_THREADS)
                      double* __restrict__ part) {
   int64_t i0, i1;
   chunk_range(n, i0, i1);
+  const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
   const T alpha = (T)scal[SCAL_ALPHA];
-  double v[2] = {0.0, 0.0};
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) {
+  DotAcc<T> a0, a1;
+  for (int64_t i = i0 + 4 * threadIdx.x; i < iv; i += 4 * DOT_THREADS) {
+    T xx[4], pp[4], rr[4], qq[4], dd[4], zz[4];
+    ldv(x + i, xx);
+    ldv(p + i, pp);
+    ldv(r + i, rr);
+    ldv(q + i, qq);
+    ldv(diag + i, dd);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      xx[k] += alpha * pp[k];
+      rr[k] = rr[k] - alpha * qq[k];
+      zz[k] = rr[k] / dd[k];
+      a0.add(rr[k], zz[k]);
+      a1.add(rr[k], rr[k]);
+    }
+    stv(x + i, xx);
+    stv(r + i, rr);
+    stv(z + i, zz);
+  }
+  for (int64_t i = iv + threadIdx.x; i < i1; i += DOT_THREADS) {
     x[i] += alpha * p[i];
     const T ri = r[i] - alpha * q[i];
     r[i] = ri;
     const T zi = ri / diag[i];
     z[i] = zi;
-    v[0] += (double)ri * (double)zi;
-    v[1] += (double)ri * (double)ri;
+    a0.add(ri, zi);
+    a1.add(ri, ri);
   }
+  double v[2] = {a0.value(), a1.value()};
   block_reduce_store<2>(v, part + 2 * blockIdx.x);
 }
 
@@ -230,8 +324,18 @@ __global__ void cg_beta_kernel(const double* __restrict__ part, double* __restri
 template <class T>
 __global__ void cg_p_kernel(int64_t n, const double* __restrict__ scal, const T* __restrict__ z,
                             T* __restrict__ p) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = z[i] + (T)scal[SCAL_BETA] * p[i];
+  const int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  const T beta = (T)scal[SCAL_BETA];
+  if (i + 3 < n) {
+    T zz[4], pp[4];
+    ldv(z + i, zz);
+    ldv(p + i, pp);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) pp[k] = zz[k] + beta * pp[k];
+    stv(p + i, pp);
+  } else {
+    for (int64_t j = i; j < n; ++j) p[j] = z[j] + beta * p[j];
+  }
 }
 
 // out = (T)(r64 / s) with s = sqrt(rr) read on the device
@@ -435,7 +539,7 @@ static int cg_iteration(const tg_operator_desc* op, T* x, const T* diag, CgBuffe
                                                           (const T*)B.p, (const T*)B.q, diag,
                                                           B.part);
   cg_beta_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal);
-  cg_p_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, B.scal, (const T*)B.z, (T*)B.p);
+  cg_p_kernel<T><<<grid_for((n + 3) / 4, 256), 256, 0, st>>>(n, B.scal, (const T*)B.z, (T*)B.p);
   return launch_check("cg iteration");
 }
 

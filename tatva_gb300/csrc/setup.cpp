@@ -79,9 +79,10 @@ struct Pattern {
 };
 
 struct Plan {
-  int32_t n_blocks = 0, n_elems = 0, npad = 4, max_local = 0, max_colors = 0, n_affine = 0;
+  int32_t n_blocks = 0, n_elems = 0, npad = 4, max_local = 0, max_colors = 0, n_affine = 0,
+          n_diag = 0, max_elems = 0;
   std::vector<int32_t> blk_elem_ptr, blk_color_ptr, color_ofs, blk_node_ptr, elem_id, lnode_gid,
-      lnode_slot, shared_node, shared_ptr, shared_slots;
+      lnode_slot, lnode_smem, shared_node, shared_ptr, shared_slots;
   std::vector<uint16_t> lconn;
 };
 
@@ -123,6 +124,73 @@ bool hex_affine_exact(const double* coords, const int32_t* nodes) {
     if (m[3] != T(0) || m[5] != T(0) || m[6] != T(0) || m[7] != T(0)) return false;
   }
   return true;
+}
+
+// Axis-aligned box test in precision T: the edge vectors at node 0 (x1 - x0, x3 - x0,
+// x4 - x0, one subtraction each, as on the device) have exact zeros off their axis.
+template <class T>
+bool hex_box_exact(const double* coords, const int32_t* nodes) {
+  const int ed[3] = {1, 3, 4};
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) {
+      if (k == i) continue;
+      const T a = (T)coords[(int64_t)nodes[ed[i]] * 3 + k];
+      const T b = (T)coords[(int64_t)nodes[0] * 3 + k];
+      if (a - b != T(0)) return false;
+    }
+  return true;
+}
+
+// Shared-memory slots of a block's local nodes.  Consecutive element positions run on
+// consecutive threads, so every run of 8 positions is one quarter-warp: the nodes it
+// reads at one element corner should sit in distinct 16-byte bank quads (slot % 8).
+// Greedy capacity-constrained 8-colouring of these groups, nodes in order of first
+// use; slot = quad + 8 * (rank within quad) < 8 ceil(nl / 8).
+void bank_aware_slots(const std::vector<int32_t>& lc_sorted, int npe, int ne, int nl,
+                      std::vector<int32_t>& slot) {
+  const int ng = ((ne + 7) / 8) * npe;
+  std::vector<int32_t> gptr(ng + 1, 0), gidx;
+  gidx.reserve((size_t)ne * npe);
+  for (int g0 = 0, gi = 0; g0 < ne; g0 += 8)
+    for (int c = 0; c < npe; ++c, ++gi) {
+      for (int k = g0; k < std::min(ne, g0 + 8); ++k) gidx.push_back(lc_sorted[(size_t)k * npe + c]);
+      gptr[gi + 1] = (int32_t)gidx.size();
+    }
+  std::vector<int32_t> nptr(nl + 1, 0), nidx(gidx.size());
+  for (int32_t v : gidx) nptr[v + 1]++;
+  for (int i = 0; i < nl; ++i) nptr[i + 1] += nptr[i];
+  {
+    std::vector<int32_t> pos(nptr.begin(), nptr.end() - 1);
+    for (int gi = 0; gi < ng; ++gi)
+      for (int k = gptr[gi]; k < gptr[gi + 1]; ++k) nidx[pos[gidx[k]]++] = gi;
+  }
+  const int cap = (nl + 7) / 8;
+  std::vector<int> quad(nl, -1), used(8, 0);
+  std::vector<char> seen(nl, 0);
+  std::vector<int32_t> order;
+  order.reserve(nl);
+  for (int32_t v : gidx)
+    if (!seen[v]) { seen[v] = 1; order.push_back(v); }
+  for (int v = 0; v < nl; ++v)
+    if (!seen[v]) order.push_back(v);
+  for (int32_t v : order) {
+    int cost[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = nptr[v]; k < nptr[v + 1]; ++k) {
+      const int gi = nidx[k];
+      for (int j = gptr[gi]; j < gptr[gi + 1]; ++j) {
+        const int o = gidx[j];
+        if (o != v && quad[o] >= 0) cost[quad[o]]++;
+      }
+    }
+    int best = -1;
+    for (int qd = 0; qd < 8; ++qd)
+      if (used[qd] < cap && (best < 0 || cost[qd] < cost[best])) best = qd;
+    quad[v] = best;
+    used[best]++;
+  }
+  int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  slot.assign(nl, 0);
+  for (int v = 0; v < nl; ++v) slot[v] = quad[v] + 8 * cnt[quad[v]]++;
 }
 
 }  // namespace
@@ -430,20 +498,26 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
     const int32_t nb = (int32_t)blk_nodes.size();
     P->n_blocks = nb;
     if (elem == TG_HEX8 && dim == 3 && nb > 0) {
-      std::vector<char> aff(nb, 1);
+      // 2: all boxes, 1: all parallelepipeds, 0: general
+      std::vector<char> kind(nb, 2);
       parallel_for(nb, [&](int64_t b0, int64_t b1, int) {
         for (int64_t b = b0; b < b1; ++b)
-          for (int32_t k = P->blk_elem_ptr[b]; k < P->blk_elem_ptr[b + 1] && aff[b]; ++k) {
+          for (int32_t k = P->blk_elem_ptr[b]; k < P->blk_elem_ptr[b + 1] && kind[b]; ++k) {
             const int32_t* nodes = conn + (int64_t)key[k].second * npe;
-            aff[b] = hex_affine_exact<double>(coords, nodes) && hex_affine_exact<float>(coords, nodes);
+            if (!(hex_affine_exact<double>(coords, nodes) && hex_affine_exact<float>(coords, nodes)))
+              kind[b] = 0;
+            else if (kind[b] == 2 &&
+                     !(hex_box_exact<double>(coords, nodes) && hex_box_exact<float>(coords, nodes)))
+              kind[b] = 1;
           }
       });
       std::vector<int32_t> order;
-      for (int32_t b = 0; b < nb; ++b)
-        if (aff[b]) order.push_back(b);
-      P->n_affine = (int32_t)order.size();
-      for (int32_t b = 0; b < nb; ++b)
-        if (!aff[b]) order.push_back(b);
+      for (int want = 2; want >= 0; --want) {
+        for (int32_t b = 0; b < nb; ++b)
+          if (kind[b] == want) order.push_back(b);
+        if (want == 2) P->n_diag = (int32_t)order.size();
+        if (want == 1) P->n_affine = (int32_t)order.size();
+      }
       std::vector<std::pair<uint64_t, int32_t>> key2;
       key2.reserve(n_elems);
       std::vector<int32_t> ptr2(1, 0), nodes2;
@@ -461,6 +535,7 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
     const int64_t total_local = P->blk_node_ptr[nb];
     P->lnode_gid.assign(total_local, 0);
     P->lnode_slot.assign(total_local, -1);
+    P->lnode_smem.assign(total_local, 0);
     P->elem_id.assign(n_elems, 0);
     P->lconn.assign(n_elems * npad, 0);
     // global degree of every node
@@ -525,14 +600,23 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
         for (int c = 0; c < nc; ++c) cofs[c + 1] += cofs[c];
         blk_colors[b] = cofs;
         std::vector<int32_t> pos(cofs.begin(), cofs.end() - 1);
+        std::vector<int32_t> lc_sorted((size_t)ne * npe);
         for (int32_t k = 0; k < ne; ++k) {
           const int32_t e = key[e0 + k].second;
-          const int32_t dst = e0 + pos[ecol[k]]++;
-          P->elem_id[dst] = e;
+          const int32_t r = pos[ecol[k]]++;
+          P->elem_id[e0 + r] = e;
           for (int a = 0; a < npe; ++a)
-            P->lconn[(int64_t)dst * npad + a] = (uint16_t)lid[conn[(int64_t)e * npe + a]];
+            lc_sorted[(size_t)r * npe + a] = lid[conn[(int64_t)e * npe + a]];
+        }
+        std::vector<int32_t> smem_slot;
+        bank_aware_slots(lc_sorted, npe, ne, (int)ids.size(), smem_slot);
+        for (int32_t r = 0; r < ne; ++r) {
+          const int32_t dst = e0 + r;
+          for (int a = 0; a < npe; ++a)
+            P->lconn[(int64_t)dst * npad + a] = (uint16_t)smem_slot[lc_sorted[(size_t)r * npe + a]];
           for (int a = npe; a < npad; ++a) P->lconn[(int64_t)dst * npad + a] = 0;
         }
+        for (size_t l = 0; l < ids.size(); ++l) P->lnode_smem[n0 + l] = smem_slot[l];
         int32_t nsh = 0;
         for (size_t l = 0; l < ids.size(); ++l) {
           const int32_t g = ids[l];
@@ -560,6 +644,7 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
       P->blk_color_ptr[b + 1] = P->blk_color_ptr[b] + (int32_t)blk_colors[b].size();
       P->max_colors = std::max<int32_t>(P->max_colors, (int32_t)blk_colors[b].size() - 1);
       P->max_local = std::max<int32_t>(P->max_local, blk_nodes[b]);
+      P->max_elems = std::max<int32_t>(P->max_elems, P->blk_elem_ptr[b + 1] - P->blk_elem_ptr[b]);
     }
     P->color_ofs.reserve(P->blk_color_ptr[nb]);
     for (int32_t b = 0; b < nb; ++b)
@@ -611,13 +696,16 @@ extern "C" int tg_plan_sizes(const void* handle, int64_t* s) {
   s[7] = P->max_colors;
   s[8] = P->npad;
   s[9] = P->n_affine;
+  s[10] = P->n_diag;
+  s[11] = P->max_elems;
   return TG_OK;
 }
 
 extern "C" int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t* blk_color_ptr,
                               int32_t* color_ofs, int32_t* blk_node_ptr, uint16_t* lconn,
                               int32_t* elem_id, int32_t* lnode_gid, int32_t* lnode_slot,
-                              int32_t* shared_node, int32_t* shared_ptr, int32_t* shared_slots) {
+                              int32_t* lnode_smem, int32_t* shared_node, int32_t* shared_ptr,
+                              int32_t* shared_slots) {
   if (!handle) return set_error(TG_ERR_VALUE, "NULL handle");
   const Plan* P = static_cast<const Plan*>(handle);
   auto cp = [](auto* dst, const auto& v) {
@@ -631,6 +719,7 @@ extern "C" int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t
   cp(elem_id, P->elem_id);
   cp(lnode_gid, P->lnode_gid);
   cp(lnode_slot, P->lnode_slot);
+  cp(lnode_smem, P->lnode_smem);
   cp(shared_node, P->shared_node);
   cp(shared_ptr, P->shared_ptr);
   cp(shared_slots, P->shared_slots);

@@ -33,9 +33,10 @@ class BlockPlan:
                                    xyz.ctypes.data, xyz.shape[1], self.block_elems,
                                    self.max_local_nodes, ctypes.byref(h)))
         try:
-            sizes = np.zeros(10, dtype=np.int64)
+            sizes = np.zeros(12, dtype=np.int64)
             _lib.check(L.tg_plan_sizes(h, sizes.ctypes.data))
-            nb, ne, ncol, nloc, nsh, npart, maxl, maxc, npad, naff = (int(x) for x in sizes)
+            nb, ne, ncol, nloc, nsh, npart, maxl, maxc, npad, naff, ndiag, maxe = (
+                int(x) for x in sizes)
             host = {
                 "blk_elem_ptr": np.zeros(nb + 1, np.int32),
                 "blk_color_ptr": np.zeros(nb + 1, np.int32),
@@ -45,20 +46,22 @@ class BlockPlan:
                 "elem_id": np.zeros(max(ne, 1), np.int32),
                 "lnode_gid": np.zeros(max(nloc, 1), np.int32),
                 "lnode_slot": np.zeros(max(nloc, 1), np.int32),
+                "lnode_smem": np.zeros(max(nloc, 1), np.int32),
                 "shared_node": np.zeros(max(nsh, 1), np.int32),
                 "shared_ptr": np.zeros(nsh + 1, np.int32),
                 "shared_slots": np.zeros(max(npart, 1), np.int32),
             }
             order = ["blk_elem_ptr", "blk_color_ptr", "color_ofs", "blk_node_ptr", "lconn",
-                     "elem_id", "lnode_gid", "lnode_slot", "shared_node", "shared_ptr",
-                     "shared_slots"]
+                     "elem_id", "lnode_gid", "lnode_slot", "lnode_smem", "shared_node",
+                     "shared_ptr", "shared_slots"]
             _lib.check(L.tg_plan_export(h, *[host[k].ctypes.data for k in order]))
         finally:
             L.tg_plan_free(h)
         self.host = host
         self.sizes = dict(n_blocks=nb, n_elems=ne, color_ofs=ncol, local_nodes=nloc,
                           n_shared=nsh, n_partials=npart, max_local_nodes=maxl,
-                          max_block_colors=maxc, stride=npad, n_affine_blocks=naff)
+                          max_block_colors=maxc, stride=npad, n_affine_blocks=naff,
+                          n_diag_blocks=ndiag, max_block_elems=maxe)
         self.device = torch.device(device)
         self.dev = {k: torch.from_numpy(v).to(self.device) for k, v in host.items()}
         s = _lib.BlockPlan()
@@ -66,6 +69,8 @@ class BlockPlan:
         s.max_local_nodes, s.n_shared, s.n_partials = maxl, nsh, npart
         s.threads = int(threads)
         s.n_affine_blocks = naff
+        s.n_diag_blocks = ndiag
+        s.max_block_elems = maxe
         for k in order:
             setattr(s, k, self.dev[k].data_ptr())
         self.struct = s

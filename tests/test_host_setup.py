@@ -115,9 +115,14 @@ def test_block_plan_invariants(elem, case, block):
         assert e1 - e0 <= block
         gid = h["lnode_gid"][n0:n1]
         assert np.all(np.diff(gid) > 0)  # sorted unique
+        smem = h["lnode_smem"][n0:n1]
+        nl = n1 - n0
+        assert len(np.unique(smem)) == nl and smem.min() >= 0 and smem.max() < 8 * ((nl + 7) // 8)
+        inv = np.full(8 * ((nl + 7) // 8), -1)
+        inv[smem] = np.arange(nl)
         for k in range(e0, e1):
-            lc = h["lconn"][k * npad:k * npad + npe].astype(np.int64)
-            np.testing.assert_array_equal(gid[lc], e[h["elem_id"][k]])
+            lc = h["lconn"][k * npad:k * npad + npe].astype(np.int64)  # shared-memory slots
+            np.testing.assert_array_equal(gid[inv[lc]], e[h["elem_id"][k]])
         # colour classes: no two elements of one colour share a node
         c0, c1 = h["blk_color_ptr"][b], h["blk_color_ptr"][b + 1]
         ofs = h["color_ofs"][c0:c1]

@@ -204,6 +204,21 @@ TG_API int tg_apply(int elem, int prec, int mode, const tg_material* mat, const 
              const void* coords, int64_t n_nodes, const void* u, const void* v,
              const uint8_t* fixed, void* y, void* workspace, size_t workspace_bytes,
              void* stream);
+/* tg_apply without a workspace argument, for callers that may not allocate device
+ * memory (a custom call running inside a runtime that owns the device heap, or a
+ * loop where cudaMalloc's device synchronisation is not acceptable).  No counterpart
+ * in the reference: it exists only for this C ABI.  The partial slots live in one
+ * fixed array of TG_NOALLOC_SCRATCH_BYTES per device inside the library; plans whose
+ * tg_apply_workspace_bytes exceed it are rejected with TG_ERR_WORKSPACE.  Nothing in
+ * the array needs to start at zero (each slot is written before it is read).  The
+ * first call on a device looks the array's address up and caches it: make that call
+ * before any stream capture.  Calls that overlap on the GPU share the array and
+ * race; calls ordered on one stream are safe.  Allocates nothing.              */
+#define TG_NOALLOC_SCRATCH_BYTES (8u << 20)
+TG_API int tg_apply_noalloc(int elem, int prec, int mode, const tg_material* mat,
+                            const tg_block_plan* plan, const void* coords, int64_t n_nodes,
+                            const void* u, const void* v, const uint8_t* fixed, void* y,
+                            void* stream);
 /* Per-element energies (n_elems,) in original element order (E(u) before the sum). */
 TG_API int tg_energy_per_element(int elem, int prec, const tg_material* mat, const void* coords,
                           int64_t n_nodes, const int32_t* conn, int64_t n_elems,

@@ -17,6 +17,10 @@
 //   * DIAG instantiation: blocks whose elements are axis-aligned boxes (verified on
 //     the host in FP32 and FP64) have a diagonal Jacobian, and the monomial terms
 //     reduce to per-component products.
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "tg_common.cuh"
 #include "tg_f32x2.cuh"
 #include "tg_internal.h"
@@ -28,6 +32,7 @@ constexpr int P6_NPT = 6;  // staged nodes per thread per block
 constexpr int P6_EPT = 4;  // element positions per thread per block
 constexpr int P6_MAX_LOCAL = P6_THREADS * P6_NPT;
 constexpr int P6_MAX_ELEMS = P6_THREADS * P6_EPT;
+constexpr int P6_CRING = 132;  // colour-offset ring entry (<= 128 colours + 1)
 
 __device__ __forceinline__ int hex_t6(int a) {
   return (a == 2) ? 3 : (a == 3) ? 2 : (a == 6) ? 7 : (a == 7) ? 6 : a;
@@ -243,7 +248,8 @@ __device__ __forceinline__ void unpack_lconn(uint4 v, int (&l)[8]) {
 // shared-memory layout (32-bit words), nl8 = node slots (multiple of 8):
 //   data buffer s (s = 0, 1) at s * 8 nl8: X (4 nl8) | W (4 nl8)
 //   node-id ring r (r = 0, 1) at 16 nl8 + r nl8, slot ring r at 18 nl8 + r nl8
-//   Y at 20 nl8 (4 nl8)                                            total 24 nl8
+//   Y at 20 nl8 (4 nl8)
+//   colour-offset ring r at 24 nl8 + r P6_CRING          total 24 nl8 + 2 P6_CRING
 template <int MODE, bool DIAG>
 __global__ void __launch_bounds__(P6_THREADS, 3)
     hex_le_f32x2_kernel(const tg_block_plan p, int b_begin, int b_end,
@@ -255,7 +261,9 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
   int* const ring = reinterpret_cast<int*>(sm + 16 * nl8);
   int* const qring = reinterpret_cast<int*>(sm + 18 * nl8);
   float* const Ybuf = sm + 20 * nl8;
+  int* const cring = reinterpret_cast<int*>(sm + 24 * nl8);
   const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
   constexpr int NT = P6_THREADS;
   const int nblk = b_end - b_begin;
   const int stride = gridDim.x;
@@ -282,21 +290,26 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
       }
     }
   };
-  // gather coordinates and input values of block b (ids in ring slot r) into buffer s
+  // colour offsets of block b (at most 129 values) into colour ring entry r
+  auto issue_cofs = [&](int b, int r) {
+    const int c0 = __ldg(p.blk_color_ptr + b), nc1 = __ldg(p.blk_color_ptr + b + 1) - c0;
+    for (int l = tid; l < nc1; l += NT) cp_async4(cring + r * P6_CRING + l, p.color_ofs + c0 + l);
+  };
+  // gather coordinates and input values of block b (ids in ring slot r) into buffer s.
+  // One warp instruction copies 8 consecutive local nodes x 3 components (lanes 0-23):
+  // the plan puts such 8 nodes in distinct 16-byte bank quads, so the 24 shared-memory
+  // words written land in 24 distinct banks, and the global reads stay contiguous.
   auto issue_data = [&](int b, int r, int s) {
     float* X = sm + s * 8 * nl8;
     float* W = X + 4 * nl8;
     const int nl = __ldg(p.blk_node_ptr + b + 1) - __ldg(p.blk_node_ptr + b);
-#pragma unroll
-    for (int k = 0; k < P6_NPT; ++k) {
-      const int l = tid + k * NT;
-      if (l < nl) {
+    const int sub = lane / 3, d = lane - 3 * sub;
+    if (lane < 24) {
+      for (int l = warp * 8 + sub; l < nl; l += (NT / 32) * 8) {
         const int q = qring[r * nl8 + l];
         const int64_t g = ring[r * nl8 + l];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) cp_async4(X + q * 4 + d, coords + g * 3 + d);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) cp_async4(W + q * 4 + d, fin + g * 3 + d);
+        cp_async4(X + q * 4 + d, coords + g * 3 + d);
+        cp_async4(W + q * 4 + d, fin + g * 3 + d);
       }
     }
   };
@@ -313,11 +326,13 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
   // prologue: ids of the first block, then its data and the ids of the second
   int bi = blockIdx.x;
   if (bi < nblk) issue_ids(b_begin + bi, 0);
+  if (bi < nblk) issue_cofs(b_begin + bi, 0);
   cp_async_commit();
   cp_async_wait0();
   __syncthreads();
   if (bi < nblk) issue_data(b_begin + bi, 0, 0);
   if (bi + stride < nblk) issue_ids(b_begin + bi + stride, 1);
+  if (bi + stride < nblk) issue_cofs(b_begin + bi + stride, 1);
   cp_async_commit();
   uint4 LC[P6_EPT];
   if (bi < nblk) load_lconn4(b_begin + bi, LC);
@@ -358,8 +373,8 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
     }
 
     const int ne = __ldg(p.blk_elem_ptr + b + 1) - __ldg(p.blk_elem_ptr + b);
-    const int c_begin = __ldg(p.blk_color_ptr + b);
-    const int c_last = __ldg(p.blk_color_ptr + b + 1) - 1;
+    const int n_col = __ldg(p.blk_color_ptr + b + 1) - 1 - __ldg(p.blk_color_ptr + b);
+    const int* const cofs = cring + s * P6_CRING;
 #pragma unroll
     for (int ch = 0; ch < P6_EPT / 2; ++ch) {
       const int k0 = ch * 2 * NT;
@@ -423,9 +438,9 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
           for (int a = 0; a < 8; ++a) f2_split(dM[j][hex_t6(a)], YA[a][j], YB[a][j]);
         }
       }
-      for (int c = c_begin; c < c_last; ++c) {
-        const int lo = max(__ldg(p.color_ofs + c), k0);
-        const int hi = min(__ldg(p.color_ofs + c + 1), k0 + 2 * NT);
+      for (int c = 0; c < n_col; ++c) {
+        const int lo = max(cofs[c], k0);
+        const int hi = min(cofs[c + 1], k0 + 2 * NT);
         if (lo >= hi) continue;  // uniform over the block
         if (actA && kA >= lo && kA < hi) {
 #pragma unroll
@@ -471,24 +486,51 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
         for (int d = 0; d < 3; ++d) partials[(int64_t)Swb[k] * 3 + d] = vals[d];
       }
     }
-    __syncthreads();
+    __syncthreads();  // every read of colour ring entry s is done
+    if (bi + 2 * stride < nblk) issue_cofs(b + 2 * stride, s);
+    cp_async_commit();
   }
   cp_async_wait0();
+}
+
+// Per (kernel, device, shared-memory size): SM count and resident CTAs per SM, set up
+// once (the attribute call and the occupancy query cost more than a launch).
+static int launch_shape(const void* k, size_t smem, int& sms, int& per_sm) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, size_t>, std::pair<int, int>> cache;
+  int dev = 0;
+  TG_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  std::lock_guard<std::mutex> g(mu);
+  const auto key = std::make_tuple(k, dev, smem);
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    int optin = 0, n_sm = 0, occ = 0;
+    TG_TRY(cuda_check(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev), "SM count"));
+    TG_TRY(cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+                      "shared memory limit"));
+    if (smem <= (size_t)optin) {
+      TG_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "hex f32x2: shared memory attribute"));
+      TG_TRY(cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, P6_THREADS, smem),
+                        "hex f32x2: occupancy"));
+    }
+    it = cache.emplace(key, std::make_pair(n_sm, occ)).first;
+  }
+  sms = it->second.first;
+  per_sm = it->second.second;
+  return TG_OK;
 }
 
 template <int MODE, bool DIAG>
 static int launch6(const tg_block_plan* plan, int b0, int b1, const float* coords,
                    const float* fin, const uint8_t* fixed, const float* vin, float* y,
-                   float* partials, float mu, float lam, int nl8, size_t smem, int sms,
-                   cudaStream_t st) {
+                   float* partials, float mu, float lam, int nl8, size_t smem, cudaStream_t st) {
   if (b1 <= b0) return TG_OK;
   auto k = hex_le_f32x2_kernel<MODE, DIAG>;
-  TG_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                    "hex f32x2: shared memory attribute"));
-  int per_sm = 0;
-  TG_TRY(cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P6_THREADS, smem),
-                    "hex f32x2: occupancy"));
-  const int grid = std::max(1, std::min(b1 - b0, sms * std::max(per_sm, 1)));
+  int sms = 0, per_sm = 0;
+  TG_TRY(launch_shape((const void*)k, smem, sms, per_sm));
+  if (per_sm <= 0) return TG_ERR_UNSUPPORTED;
+  const int grid = std::max(1, std::min(b1 - b0, sms * per_sm));
   k<<<grid, P6_THREADS, smem, st>>>(*plan, b0, b1, coords, fin, fixed, vin, y, partials, mu, lam,
                                     nl8);
   return launch_check("hex f32x2 kernel");
@@ -503,23 +545,17 @@ int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords
     return TG_ERR_UNSUPPORTED;
   if (n_diag < 0 || n_diag > n_aff) return set_error(TG_ERR_VALUE, "plan.n_diag_blocks out of range");
   const int nl8 = (plan->max_local_nodes + 7) & ~7;
-  const size_t smem = (size_t)24 * nl8 * sizeof(float);
-  int dev = 0, sms = 0, optin = 0;
-  TG_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
-  TG_TRY(cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
-  TG_TRY(cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
-                    "shared memory limit"));
-  if (smem > (size_t)optin) return TG_ERR_UNSUPPORTED;
+  const size_t smem = ((size_t)24 * nl8 + 2 * P6_CRING) * sizeof(float);
   if (mode == TG_MODE_HVP) {
     TG_TRY((launch6<TG_MODE_HVP, true>(plan, 0, n_diag, coords, v, fixed, v, y, partials, mu, lam,
-                                       nl8, smem, sms, st)));
+                                       nl8, smem, st)));
     return launch6<TG_MODE_HVP, false>(plan, n_diag, n_aff, coords, v, fixed, v, y, partials, mu,
-                                       lam, nl8, smem, sms, st);
+                                       lam, nl8, smem, st);
   }
   TG_TRY((launch6<TG_MODE_RESIDUAL, true>(plan, 0, n_diag, coords, u, fixed, v, y, partials, mu,
-                                          lam, nl8, smem, sms, st)));
+                                          lam, nl8, smem, st)));
   return launch6<TG_MODE_RESIDUAL, false>(plan, n_diag, n_aff, coords, u, fixed, v, y, partials,
-                                          mu, lam, nl8, smem, sms, st);
+                                          mu, lam, nl8, smem, st);
 }
 
 }  // namespace tg

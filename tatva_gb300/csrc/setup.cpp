@@ -144,8 +144,10 @@ bool hex_box_exact(const double* coords, const int32_t* nodes) {
 // Shared-memory slots of a block's local nodes.  Consecutive element positions run on
 // consecutive threads, so every run of 8 positions is one quarter-warp: the nodes it
 // reads at one element corner should sit in distinct 16-byte bank quads (slot % 8).
-// Greedy capacity-constrained 8-colouring of these groups, nodes in order of first
-// use; slot = quad + 8 * (rank within quad) < 8 ceil(nl / 8).
+// The same holds for every run of 8 consecutive local nodes, which one warp
+// instruction copies into shared memory.  Greedy capacity-constrained 8-colouring of
+// both kinds of groups, nodes in order of first use; slot = quad + 8 * (rank within
+// quad) < 8 ceil(nl / 8).
 void bank_aware_slots(const std::vector<int32_t>& lc_sorted, int npe, int ne, int nl,
                       std::vector<int32_t>& slot) {
   const int ng = ((ne + 7) / 8) * npe;
@@ -182,6 +184,9 @@ void bank_aware_slots(const std::vector<int32_t>& lc_sorted, int npe, int ne, in
         if (o != v && quad[o] >= 0) cost[quad[o]]++;
       }
     }
+    // staging group: the 8 consecutive local nodes that one warp instruction copies
+    for (int o = v & ~7; o < std::min(nl, (v & ~7) + 8); ++o)
+      if (o != v && quad[o] >= 0) cost[quad[o]]++;
     int best = -1;
     for (int qd = 0; qd < 8; ++qd)
       if (used[qd] < cap && (best < 0 || cost[qd] < cost[best])) best = qd;

@@ -66,29 +66,9 @@ def _traffic_from_profile():
 
 
 def brick_problem(n, device):
-    import torch
+    from tatva_gb300.problems import clamped_brick
 
-    from tatva_gb300 import Mesh, Operator, element, materials
-
-    mesh = Mesh.brick(n, n, n, device=device)
-    op = Operator(mesh, element.Hexahedron8())
-    en = materials.LinearElastic.from_young(op, 1.0, 0.3)
-    c = mesh.coords_host()
-    nn = c.shape[0]
-    fixed = np.zeros(nn * 3, np.uint8)
-    left = np.where(c[:, 0] == 0.0)[0]
-    for k in range(3):
-        fixed[left * 3 + k] = 1
-    # consistent nodal forces of a uniform traction t = 1e-3 e_x on x = 1
-    b = np.zeros(nn * 3)
-    h = 1.0 / n
-    right = np.where(c[:, 0] == 1.0)[0]
-    jy = np.rint(c[right, 1] / h).astype(int)
-    jz = np.rint(c[right, 2] / h).astype(int)
-    mult = (np.where((jy == 0) | (jy == n), 1, 2) * np.where((jz == 0) | (jz == n), 1, 2))
-    b[right * 3] = 1e-3 * (h * h / 4) * mult
-    return dict(mesh=mesh, op=op, energy=en, fixed=torch.as_tensor(fixed, device=device),
-                b=torch.as_tensor(b, device=device), n_nodes=nn, n_elems=mesh.n_elements)
+    return clamped_brick(n, device, traction=1e-3)
 
 
 class ClockSampler:

@@ -225,6 +225,49 @@ TG_API int tg_energy_per_element(int elem, int prec, const tg_material* mat, con
                           const void* u, void* out, void* stream);
 
 /* ============================================================================
+ * Batched solves: many independent SPD systems (one per mesh) in one persistent
+ * launch.  No single counterpart in the reference, where a user loops over meshes
+ * and calls jax.scipy.sparse.linalg.cg per mesh (README.md:93) on the matrix that
+ * tatva.sparse.jacfwd assembles (tatva/sparse/base.py:139-176).
+ *
+ * The systems are the diagonal blocks of one block-diagonal CSR matrix (rows
+ * row_ofs[s] .. row_ofs[s+1]-1 couple only among themselves), stored per system as
+ * column-major ELLPACK of width ell_width[s] starting at entry ell_ofs[s]: entry k of
+ * local row i at ell_ofs[s] + k * n_s + i, 16-bit local column ids, padding entries
+ * (value 0) point at the row itself.                                          */
+typedef struct tg_batch_desc {
+  int32_t n_systems;
+  int32_t max_rows;           /* largest n_s (<= 49152) */
+  const int64_t* row_ofs;     /* (n_systems + 1) */
+  const int64_t* ell_ofs;     /* (n_systems) */
+  const int32_t* ell_width;   /* (n_systems) */
+  const int32_t* order;       /* (n_systems) order in which CTAs take systems */
+  const uint16_t* ell_col;
+  const float* ell_val32;
+  const double* ell_val64;
+} tg_batch_desc;
+/* Fill ell_col / ell_val32 / ell_val64 (written through the descriptor's pointers)
+ * from the block-diagonal CSR (int32 indptr/indices, FP64 data).  *bad_flag (device
+ * int, zeroed by the caller) becomes 1 when a row is longer than its system's width
+ * and 2 when a row couples to another system.                                  */
+TG_API int tg_batch_ell_from_csr(const tg_batch_desc* desc, int64_t n_rows, const int32_t* indptr,
+                                 const int32_t* indices, const double* data, int32_t* bad_flag,
+                                 void* stream);
+TG_API size_t tg_batch_workspace_bytes(int64_t n_rows);
+/* Solve A_s x_s = b_s for every system (x overwritten, starting from 0): FP32
+ * Jacobi-CG inner solves on r64/|r64| to inner_rtol, FP64 refinement on the true
+ * residual until |b - A64 x| <= rtol |b|.  One CTA of `threads` (128, 256, 512)
+ * threads per system at a time, at most ctas_per_sm CTAs per SM (0: as many as fit).
+ * Per system (device arrays): total inner iterations, refinements, final relative
+ * residual, status (TG_OK, TG_ERR_NOT_CONVERGED, TG_ERR_BREAKDOWN, TG_ERR_VALUE).
+ * The result of a system does not depend on the other systems in the batch.    */
+TG_API int tg_batch_solve(const tg_batch_desc* desc, int64_t n_rows, const double* b, double* x,
+                          double rtol, double inner_rtol, int max_outer, int max_inner,
+                          int threads, int ctas_per_sm, void* workspace, size_t workspace_bytes,
+                          int32_t* iters, int32_t* outer, double* rel_res, int32_t* status,
+                          void* stream);
+
+/* ============================================================================
  * Colored compressed Hessian (K6) and CSR decompression.  Replaces
  * tatva/sparse/base.py compute_rows_cols (:108-136), colored_jacobian_batch
  * (:230-270) and the decompression data = Jc[rows, col_colors] of jacfwd /

@@ -88,6 +88,20 @@ class SolveStats(ctypes.Structure):
     ]
 
 
+class BatchDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_systems", c_int32),
+        ("max_rows", c_int32),
+        ("row_ofs", c_void_p),
+        ("ell_ofs", c_void_p),
+        ("ell_width", c_void_p),
+        ("order", c_void_p),
+        ("ell_col", c_void_p),
+        ("ell_val32", c_void_p),
+        ("ell_val64", c_void_p),
+    ]
+
+
 class OperatorDesc(ctypes.Structure):
     _fields_ = [
         ("elem", c_int32),
@@ -157,6 +171,9 @@ SIGNATURES = {
     "tg_cg_solve": (I, [P, P, P, P, D, I, I, P, S, P, P]),
     "tg_mixed_workspace_bytes": (S, [P, P]),
     "tg_mixed_solve": (I, [P, P, P, P, P, D, D, I, I, I, P, S, P, P]),
+    "tg_batch_ell_from_csr": (I, [P, L, P, P, P, P, P]),
+    "tg_batch_workspace_bytes": (S, [L]),
+    "tg_batch_solve": (I, [P, L, P, P, D, D, I, I, I, I, P, S, P, P, P, P, P]),
     "tg_pattern_build": (I, [P, L, I, L, I, POINTER(c_void_p)]),
     "tg_pattern_nnz": (I, [P, P]),
     "tg_pattern_export": (I, [P, P, P]),

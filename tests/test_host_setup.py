@@ -167,3 +167,32 @@ def test_element_colors_and_incidence():
         ent = ix[ip[n]:ip[n + 1]]
         assert np.all(e.reshape(-1)[ent] == n) and np.all(np.diff(ent) > 0)
         assert len(ent) == np.sum(e == n)
+
+
+def test_batch_helpers_boundary_and_concat():
+    from tatva_gb300 import batched
+
+    c, e = om.unit_square(5, 3)
+    mask = batched.boundary_nodes_tri3(e, c.shape[0])
+    geo = (np.isclose(c[:, 0], 0) | np.isclose(c[:, 0], 1) | np.isclose(c[:, 1], 0)
+           | np.isclose(c[:, 1], 1))
+    np.testing.assert_array_equal(mask, geo)
+    c2, e2 = om.unit_square(2, 2)
+    cc, ee, nofs, eofs = batched.concat_meshes([(c, e), (c2, e2)])
+    assert list(nofs) == [0, c.shape[0], c.shape[0] + c2.shape[0]]
+    assert list(eofs) == [0, e.shape[0], e.shape[0] + e2.shape[0]]
+    np.testing.assert_array_equal(ee[e.shape[0]:], e2 + c.shape[0])
+    meshes, kappas, sides = batched.random_unit_squares(64, seed=5)
+    assert sides.min() >= 8 and sides.max() <= 96 and len(meshes) == 64
+    assert all(k.shape[0] == 2 * n * n for k, n in zip(kappas, sides))
+
+
+def test_synthetic_request_stream():
+    from tatva_gb300 import serving
+
+    reqs = serving.synthetic_requests(2000, rate=2000.0, seed=0)
+    arr = np.array([r.arrival for r in reqs])
+    assert arr[0] == 0.0 and np.all(np.diff(arr) >= 0)
+    assert 0.8 < (len(arr) - 1) / arr[-1] / 2000.0 < 1.2
+    assert {r.side for r in reqs} == {16, 24, 32, 48, 64}
+    assert all(0.2 <= r.poisson <= 0.45 for r in reqs)

@@ -158,6 +158,10 @@ typedef struct tg_block_plan {
   const int32_t* shared_node;    /* [n_shared] global node id                      */
   const int32_t* shared_ptr;     /* [n_shared+1]                                   */
   const int32_t* shared_slots;   /* [n_partials] slots in summation order          */
+  /* optional, FP32 linear elasticity on Hex8 boxes: [3][n_elems] edge terms
+   * 4(x1-x0), 4(y3-y0), 4(z4-z0) of the element positions of the box blocks, filled
+   * by tg_plan_box_geometry; NULL: the kernel computes them from coordinates.     */
+  const float* box_geom32;
 } tg_block_plan;
 
 /* Material parameters.  kind = TG_POISSON: p0 = kappa, p1 = f (source);
@@ -189,6 +193,10 @@ TG_API int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t* bl
                    int32_t* lnode_smem, int32_t* shared_node, int32_t* shared_ptr,
                    int32_t* shared_slots);
 TG_API void tg_plan_free(void* handle);
+/* Fill box_geom32 (device, 3 * n_elems floats) from FP32 coordinates and the int32
+ * connectivity; identical in every bit to what the kernel derives from coordinates. */
+TG_API int tg_plan_box_geometry(const tg_block_plan* plan, const float* coords, const int32_t* conn,
+                                float* out, void* stream);
 
 /* y = mode(u, v) over the plan:
  *   RESIDUAL  y = dE/du (u)               v unused

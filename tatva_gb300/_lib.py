@@ -63,6 +63,7 @@ class BlockPlan(ctypes.Structure):
         ("shared_node", c_void_p),
         ("shared_ptr", c_void_p),
         ("shared_slots", c_void_p),
+        ("box_geom32", c_void_p),
     ]
 
 
@@ -149,6 +150,7 @@ SIGNATURES = {
     "tg_plan_sizes": (I, [P, P]),
     "tg_plan_export": (I, [P] + [P] * 12),
     "tg_plan_free": (None, [P]),
+    "tg_plan_box_geometry": (I, [P, P, P, P, P]),
     "tg_apply_workspace_bytes": (S, [I, I, I, P]),
     "tg_apply": (I, [I, I, I, P, P, P, L, P, P, P, P, P, S, P]),
     "tg_apply_noalloc": (I, [I, I, I, P, P, P, L, P, P, P, P, P]),

@@ -86,3 +86,23 @@ def load(path: str) -> None:
     with open(path) as f:
         for k, v in json.load(f):
             _TABLE[tuple(k)] = tuple(v)
+
+
+def tune_batch(systems, b, candidates=((128, 0), (256, 0), (512, 0), (256, 2), (512, 2)),
+               **solve_kw):
+    """Pick threads per CTA and CTAs per SM of ``tg_batch_solve`` by timing one full
+    batched solve per candidate; the choice is stored on ``systems``."""
+    bb = b.reshape(-1).to(torch.float64).contiguous()
+    x = torch.empty_like(bb)
+    results = []
+    for threads, cps in candidates:
+        systems.launch(bb, x, threads=threads, ctas_per_sm=cps, **solve_kw)  # warm
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        systems.launch(bb, x, threads=threads, ctas_per_sm=cps, **solve_kw)
+        e.record()
+        e.synchronize()
+        results.append((s.elapsed_time(e), threads, cps))
+    results.sort()
+    systems.threads, systems.ctas_per_sm = results[0][1], results[0][2]
+    return [dict(ms=r[0], threads=r[1], ctas_per_sm=r[2]) for r in results]

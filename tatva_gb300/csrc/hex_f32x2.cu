@@ -22,6 +22,7 @@
 #include <tuple>
 
 #include "tg_common.cuh"
+#include "tg_dispatch.cuh"
 #include "tg_f32x2.cuh"
 #include "tg_internal.h"
 
@@ -245,23 +246,38 @@ __device__ __forceinline__ void unpack_lconn(uint4 v, int (&l)[8]) {
   l[4] = v.z & 0xffff; l[5] = v.z >> 16; l[6] = v.w & 0xffff; l[7] = v.w >> 16;
 }
 
-// shared-memory layout (32-bit words), nl8 = node slots (multiple of 8):
-//   data buffer s (s = 0, 1) at s * 8 nl8: X (4 nl8) | W (4 nl8)
-//   node-id ring r (r = 0, 1) at 16 nl8 + r nl8, slot ring r at 18 nl8 + r nl8
-//   Y at 20 nl8 (4 nl8)
-//   colour-offset ring r at 24 nl8 + r P6_CRING          total 24 nl8 + 2 P6_CRING
-template <int MODE, bool DIAG>
-__global__ void __launch_bounds__(P6_THREADS, 3)
+// Element kinds of the kernel: general parallelepipeds (Jacobian from staged
+// coordinates), axis-aligned boxes with the edge lengths from staged coordinates, and
+// axis-aligned boxes with the edge lengths from the plan's per-element box_geom32.
+constexpr int P6_AFFINE = 0, P6_BOX = 1, P6_BOX_GEOM = 2;
+
+// words of one data buffer per node slot: X (4) and W (4), or W only
+__host__ __device__ constexpr int p6_buf_words(int kind) { return kind == P6_BOX_GEOM ? 4 : 8; }
+__host__ __device__ constexpr int p6_smem_words_per_slot(int kind) {
+  return 2 * p6_buf_words(kind) + 8;
+}
+
+// shared-memory layout (32-bit words), nl8 = node slots (multiple of 8), B = buffer
+// words per slot (8: X | W, 4: W only):
+//   data buffer s (s = 0, 1) at s * B nl8: [X (4 nl8)] | W (4 nl8)
+//   node-id ring r (r = 0, 1) at 2B nl8 + r nl8, slot ring r at (2B + 2) nl8 + r nl8
+//   Y at (2B + 4) nl8 (4 nl8)
+//   colour-offset ring r at (2B + 8) nl8 + r P6_CRING     total (2B + 8) nl8 + 2 P6_CRING
+template <int MODE, int KIND>
+__global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
     hex_le_f32x2_kernel(const tg_block_plan p, int b_begin, int b_end,
                         const float* __restrict__ coords, const float* __restrict__ fin,
                         const uint8_t* __restrict__ fixed, const float* __restrict__ vin,
                         float* __restrict__ y, float* __restrict__ partials, float mu_s,
                         float lam_s, int nl8) {
+  constexpr bool DIAG = KIND != P6_AFFINE;
+  constexpr bool GEO = KIND == P6_BOX_GEOM;
+  constexpr int BW = p6_buf_words(KIND);
   extern __shared__ __align__(16) float sm[];
-  int* const ring = reinterpret_cast<int*>(sm + 16 * nl8);
-  int* const qring = reinterpret_cast<int*>(sm + 18 * nl8);
-  float* const Ybuf = sm + 20 * nl8;
-  int* const cring = reinterpret_cast<int*>(sm + 24 * nl8);
+  int* const ring = reinterpret_cast<int*>(sm + 2 * BW * nl8);
+  int* const qring = reinterpret_cast<int*>(sm + (2 * BW + 2) * nl8);
+  float* const Ybuf = sm + (2 * BW + 4) * nl8;
+  int* const cring = reinterpret_cast<int*>(sm + (2 * BW + 8) * nl8);
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   constexpr int NT = P6_THREADS;
@@ -271,8 +287,8 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
   for (int l = tid; l < nl8; l += NT) {
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      sm[s * 8 * nl8 + l * 4 + 3] = 0.f;
-      sm[s * 8 * nl8 + 4 * nl8 + l * 4 + 3] = 0.f;
+      sm[s * BW * nl8 + l * 4 + 3] = 0.f;
+      if (!GEO) sm[s * BW * nl8 + 4 * nl8 + l * 4 + 3] = 0.f;
     }
     reinterpret_cast<float4*>(Ybuf)[l] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -300,15 +316,15 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
   // the plan puts such 8 nodes in distinct 16-byte bank quads, so the 24 shared-memory
   // words written land in 24 distinct banks, and the global reads stay contiguous.
   auto issue_data = [&](int b, int r, int s) {
-    float* X = sm + s * 8 * nl8;
-    float* W = X + 4 * nl8;
+    float* X = sm + s * BW * nl8;
+    float* W = X + (BW - 4) * nl8;
     const int nl = __ldg(p.blk_node_ptr + b + 1) - __ldg(p.blk_node_ptr + b);
     const int sub = lane / 3, d = lane - 3 * sub;
     if (lane < 24) {
       for (int l = warp * 8 + sub; l < nl; l += (NT / 32) * 8) {
         const int q = qring[r * nl8 + l];
         const int64_t g = ring[r * nl8 + l];
-        cp_async4(X + q * 4 + d, coords + g * 3 + d);
+        if (!GEO) cp_async4(X + q * 4 + d, coords + g * 3 + d);
         cp_async4(W + q * 4 + d, fin + g * 3 + d);
       }
     }
@@ -357,8 +373,9 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
     if (bi + 2 * stride < nblk) issue_ids(b + 2 * stride, s);
     cp_async_commit();
 
-    const float* X = sm + s * 8 * nl8;
-    float* W = const_cast<float*>(X) + 4 * nl8;
+    const float* X = sm + s * BW * nl8;
+    float* W = const_cast<float*>(X) + (BW - 4) * nl8;
+    const int e_blk = __ldg(p.blk_elem_ptr + b);
     if (MODE == TG_MODE_HVP && fixed) {
 #pragma unroll
       for (int k = 0; k < P6_NPT; ++k) {
@@ -387,7 +404,22 @@ __global__ void __launch_bounds__(P6_THREADS, 3)
       unpack_lconn(actB ? LC[2 * ch + 1] : LC[2 * ch], qB);
       if (actA) {
         f2 R[3][3], detJm;
-        {
+        if constexpr (GEO) {
+          const float* gp = p.box_geom32;
+          const int64_t ng = p.n_elems;
+          const int64_t iA = e_blk + kA, iB = e_blk + (actB ? kB : kA);
+          const float jA0 = __ldg(gp + iA), jB0 = __ldg(gp + iB);
+          const float jA1 = __ldg(gp + ng + iA), jB1 = __ldg(gp + ng + iB);
+          const float jA2 = __ldg(gp + 2 * ng + iA), jB2 = __ldg(gp + 2 * ng + iB);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) R[i][j] = f2_zero();
+          R[0][0] = f2_make(__frcp_rn(jA0), __frcp_rn(jB0));
+          R[1][1] = f2_make(__frcp_rn(jA1), __frcp_rn(jB1));
+          R[2][2] = f2_make(__frcp_rn(jA2), __frcp_rn(jB2));
+          detJm = f2_make(jA0 * jA1 * jA2, jB0 * jB1 * jB2);
+        } else {
           const float4 a0 = reinterpret_cast<const float4*>(X)[qA[0]];
           const float4 b0 = reinterpret_cast<const float4*>(X)[qB[0]];
           const float4 a1 = reinterpret_cast<const float4*>(X)[qA[1]];
@@ -521,12 +553,14 @@ static int launch_shape(const void* k, size_t smem, int& sms, int& per_sm) {
   return TG_OK;
 }
 
-template <int MODE, bool DIAG>
+template <int MODE, int KIND>
 static int launch6(const tg_block_plan* plan, int b0, int b1, const float* coords,
                    const float* fin, const uint8_t* fixed, const float* vin, float* y,
-                   float* partials, float mu, float lam, int nl8, size_t smem, cudaStream_t st) {
+                   float* partials, float mu, float lam, int nl8, cudaStream_t st) {
   if (b1 <= b0) return TG_OK;
-  auto k = hex_le_f32x2_kernel<MODE, DIAG>;
+  auto k = hex_le_f32x2_kernel<MODE, KIND>;
+  const size_t smem =
+      ((size_t)p6_smem_words_per_slot(KIND) * nl8 + 2 * P6_CRING) * sizeof(float);
   int sms = 0, per_sm = 0;
   TG_TRY(launch_shape((const void*)k, smem, sms, per_sm));
   if (per_sm <= 0) return TG_ERR_UNSUPPORTED;
@@ -534,6 +568,22 @@ static int launch6(const tg_block_plan* plan, int b0, int b1, const float* coord
   k<<<grid, P6_THREADS, smem, st>>>(*plan, b0, b1, coords, fin, fixed, vin, y, partials, mu, lam,
                                     nl8);
   return launch_check("hex f32x2 kernel");
+}
+
+template <int MODE>
+static int launch_modes(const tg_block_plan* plan, const float* coords, const float* fin,
+                        const uint8_t* fixed, const float* vin, float* y, float* partials,
+                        float mu, float lam, int nl8, cudaStream_t st) {
+  const int n_aff = plan->n_affine_blocks, n_diag = plan->n_diag_blocks;
+  if (plan->box_geom32) {
+    TG_TRY((launch6<MODE, P6_BOX_GEOM>(plan, 0, n_diag, coords, fin, fixed, vin, y, partials, mu,
+                                       lam, nl8, st)));
+  } else {
+    TG_TRY((launch6<MODE, P6_BOX>(plan, 0, n_diag, coords, fin, fixed, vin, y, partials, mu, lam,
+                                  nl8, st)));
+  }
+  return launch6<MODE, P6_AFFINE>(plan, n_diag, n_aff, coords, fin, fixed, vin, y, partials, mu,
+                                  lam, nl8, st);
 }
 
 int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords, const float* u,
@@ -545,17 +595,54 @@ int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords
     return TG_ERR_UNSUPPORTED;
   if (n_diag < 0 || n_diag > n_aff) return set_error(TG_ERR_VALUE, "plan.n_diag_blocks out of range");
   const int nl8 = (plan->max_local_nodes + 7) & ~7;
-  const size_t smem = ((size_t)24 * nl8 + 2 * P6_CRING) * sizeof(float);
-  if (mode == TG_MODE_HVP) {
-    TG_TRY((launch6<TG_MODE_HVP, true>(plan, 0, n_diag, coords, v, fixed, v, y, partials, mu, lam,
-                                       nl8, smem, st)));
-    return launch6<TG_MODE_HVP, false>(plan, n_diag, n_aff, coords, v, fixed, v, y, partials, mu,
-                                       lam, nl8, smem, st);
-  }
-  TG_TRY((launch6<TG_MODE_RESIDUAL, true>(plan, 0, n_diag, coords, u, fixed, v, y, partials, mu,
-                                          lam, nl8, smem, st)));
-  return launch6<TG_MODE_RESIDUAL, false>(plan, n_diag, n_aff, coords, u, fixed, v, y, partials,
-                                          mu, lam, nl8, smem, st);
+  // the general kernel needs the most shared memory: check it before launching anything
+  int sms = 0, per_sm = 0;
+  const size_t smem_aff =
+      ((size_t)p6_smem_words_per_slot(P6_AFFINE) * nl8 + 2 * P6_CRING) * sizeof(float);
+  TG_TRY(launch_shape((const void*)hex_le_f32x2_kernel<TG_MODE_HVP, P6_AFFINE>, smem_aff, sms,
+                      per_sm));
+  if (per_sm <= 0) return TG_ERR_UNSUPPORTED;
+  if (mode == TG_MODE_HVP)
+    return launch_modes<TG_MODE_HVP>(plan, coords, v, fixed, v, y, partials, mu, lam, nl8, st);
+  return launch_modes<TG_MODE_RESIDUAL>(plan, coords, u, fixed, v, y, partials, mu, lam, nl8, st);
+}
+
+// Per-element box edge terms 4 (x1 - x0), 4 (y3 - y0), 4 (z4 - z0) in FP32, exactly as
+// the box kernel computes them from staged coordinates, for element positions
+// [0, blk_elem_ptr[n_diag_blocks]) of the plan; layout [3][n_elems].
+__global__ void box_geometry_kernel(const tg_block_plan p, const float* __restrict__ coords,
+                                    const int32_t* __restrict__ conn, float* __restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= p.n_elems) return;
+  const int end = p.blk_elem_ptr[p.n_diag_blocks];
+  if (k >= end) return;
+  const int64_t e = p.elem_id[k];
+  const int32_t* c = conn + e * 8;
+  const float* x0 = coords + (int64_t)c[0] * 3;
+  const float* x1 = coords + (int64_t)c[1] * 3;
+  const float* x3 = coords + (int64_t)c[3] * 3;
+  const float* x4 = coords + (int64_t)c[4] * 3;
+  out[k] = 4.f * (x1[0] - x0[0]);
+  out[p.n_elems + k] = 4.f * (x3[1] - x0[1]);
+  out[2 * (int64_t)p.n_elems + k] = 4.f * (x4[2] - x0[2]);
 }
 
 }  // namespace tg
+
+using namespace tg;
+
+extern "C" int tg_plan_box_geometry(const tg_block_plan* plan, const float* coords,
+                                    const int32_t* conn, float* out, void* stream) {
+  if (!plan) return set_error(TG_ERR_VALUE, "plan must not be NULL");
+  if (plan->nodes_per_elem_padded != 8)
+    return set_error(TG_ERR_VALUE, "box geometry needs a Hex8 plan");
+  if (plan->n_diag_blocks < 0 || plan->n_diag_blocks > plan->n_blocks)
+    return set_error(TG_ERR_VALUE, "plan.n_diag_blocks out of range");
+  if (plan->n_elems == 0 || plan->n_diag_blocks == 0) return TG_OK;
+  TG_TRY(check_ptr(coords, "coords"));
+  TG_TRY(check_ptr(conn, "conn"));
+  TG_TRY(check_ptr(out, "out"));
+  box_geometry_kernel<<<grid_for(plan->n_elems, 256), 256, 0, as_stream(stream)>>>(*plan, coords,
+                                                                                  conn, out);
+  return launch_check("tg_plan_box_geometry");
+}

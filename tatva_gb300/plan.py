@@ -74,6 +74,15 @@ class BlockPlan:
         for k in order:
             setattr(s, k, self.dev[k].data_ptr())
         self.struct = s
+        self.box_geom32 = None
+        if elem_id == _lib.TG_HEX8 and ndiag > 0 and self.device.type == "cuda":
+            # edge terms of the box elements for the FP32 box kernel (no coordinate staging)
+            x32 = torch.as_tensor(xyz, dtype=torch.float32, device=self.device)
+            c32 = torch.as_tensor(conn, device=self.device)
+            self.box_geom32 = torch.empty(3 * ne, dtype=torch.float32, device=self.device)
+            _lib.call("tg_plan_box_geometry", ctypes.byref(s), x32.data_ptr(), c32.data_ptr(),
+                      self.box_geom32.data_ptr(), torch.cuda.current_stream(self.device).cuda_stream)
+            s.box_geom32 = self.box_geom32.data_ptr()
 
     @property
     def threads(self) -> int:

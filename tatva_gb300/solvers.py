@@ -206,6 +206,9 @@ def newton(energy, u0: torch.Tensor, lifter, *, colored_matrix=None, rtol: float
         K = jac(u.to(tangent_dtype))
         sol = csr_cg(K, -r, fixed=mask, rtol=cg_rtol, raise_on_fail=False)
         total_cg += sol.iterations
+        if sol.status == _lib.TG_ERR_BREAKDOWN or not bool(torch.isfinite(sol.x).all()):
+            status = _lib.TG_ERR_BREAKDOWN  # indefinite tangent: stop, keep the last iterate
+            break
         u = u + sol.x.to(torch.float64)
     torch.cuda.synchronize()
     res = SolveResult(u.view(u0.shape), total_cg, it, hist[-1] / max(hist[0], 1e-300), status,

@@ -147,6 +147,35 @@ def test_hex_brick_affine_and_general(cuda, shape, jitter, kind):
                omat.hvp(oo, law, u, v)) < 1e-4
 
 
+def test_hex_box_geometry_path_is_bitwise_equal(cuda):
+    """FP32 box kernel with the plan's precomputed edge terms (box_geom32) equals the
+    kernel that derives them from staged coordinates, bit for bit; both match the
+    oracle.  Uneven box sizes so that the edge terms differ per element."""
+    xs = np.cumsum(np.r_[0.0, np.linspace(0.5, 1.5, 9)])
+    c, e = om.brick(9, 7, 6)
+    c = c * np.array([9.0, 7.0, 6.0])
+    c[:, 0] = xs[np.rint(c[:, 0]).astype(int)]
+    op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    plan = op.plan(128, 4096, 128)
+    assert plan.sizes["n_diag_blocks"] == plan.sizes["n_blocks"] and plan.box_geom32 is not None
+    en = materials.LinearElastic(op, 0.7, 1.9)
+    en.use_plan(plan)
+    rng = np.random.default_rng(5)
+    v = _t(rng.standard_normal(en.n_dofs), cuda, torch.float32)
+    u = _t(0.01 * rng.standard_normal(en.n_dofs), cuda, torch.float32)
+    y_geo, r_geo = en.hvp(None, v), en.residual(u)
+    saved = plan.struct.box_geom32
+    try:
+        plan.struct.box_geom32 = None
+        y_x, r_x = en.hvp(None, v), en.residual(u)
+    finally:
+        plan.struct.box_geom32 = saved
+    assert torch.equal(y_geo, y_x) and torch.equal(r_geo, r_x)
+    oo = oop.OracleOperator(c, e, oe.Hexahedron8())
+    law = omat.LinearElastic(0.7, 1.9)
+    assert rel(y_geo, omat.hvp(oo, law, None, v.double().cpu().numpy())) < 1e-5
+
+
 @pytest.mark.parametrize("kind", ["linear_elastic", "poisson"])
 def test_hex_sheared_parallelepipeds_modal_path(cuda, kind):
     """A sheared brick with dyadic shear factors: every element is an exact

@@ -6,7 +6,8 @@ nu = 0.3, clamped x = 0 face, uniform normal traction 1e-3 on x = 1.
 
 * step: one matrix-free HVP y = K v over the whole mesh (FP32 kernel, FP32
   vectors and coordinates), inputs resident in HBM; the L2 is flushed (256 MiB
-  write) before every step and the HVP is timed with CUDA events on its stream.
+  write) before every step and the HVP -- captured once as a CUDA graph of its two
+  kernel launches and replayed -- is timed with CUDA events on its stream.
 * value: dofs per second (GDOF/s) over the K timed steps, summed over ranks.
 * e2e: the same HVP through the public API with the input copied from pinned host
   memory and the result copied back inside the timed region.
@@ -366,18 +367,102 @@ def _cpu_serving_sample():
                       f"Jacobi-CG to rel-res 1e-10, {dt:.1f} s"}
 
 
+def bench_newton(dev, args):
+    """Neo-Hookean Tet4 (Kuhn split of n^3 cells, interior jitter +-0.2h, mu=1, lambda=10),
+    20% uniaxial stretch in load steps; Newton with FP64 residual/update and the FP32
+    colored sparse tangent, CSR CG inner solves (Eisenstat-Walker tolerances)."""
+    import torch
+
+    from tatva_gb300 import sparse, solvers
+    from tatva_gb300.lifter import Fixed, Lifter
+    from tatva_gb300.problems import stretched_kuhn
+
+    n, steps = args.newton, args.newton_steps
+    t0 = time.perf_counter()
+    P = stretched_kuhn(n, dev)
+    en, c = P["energy"], P["coords"]
+    cm = sparse.ColoredMatrix.from_csr(sparse.pattern_from_mesh(P["mesh"], 3), device=dev)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    u = torch.zeros(en.n_dofs, dtype=torch.float64, device=dev)
+    hist, newton_its, cg_its = [], 0, 0
+    t1 = time.perf_counter()
+    for step in range(1, steps + 1):
+        lifter = Lifter(en.n_dofs, Fixed(P["dofs"], P["values"](0.2 * step / steps)))
+        du = torch.zeros_like(u)
+        du.view(-1, 3)[:, 0] = torch.as_tensor(c[:, 0] * (0.2 / steps), device=dev)
+        u = lifter.lift(lifter.reduce(u + du), u + du)  # affine predictor, exact lift
+        res = solvers.newton(en, u, lifter, colored_matrix=cm, rtol=1e-10, max_iter=30)
+        hist.append({"step": step, "newton": res.outer, "cg": res.iterations,
+                     "rel_res": res.rel_res, "converged": res.converged})
+        newton_its += res.outer
+        cg_its += res.iterations
+        u = res.x
+        if not res.converged:
+            break
+    total = time.perf_counter() - t1
+    out = {"workload": f"Neo-Hookean Tet4, Kuhn {n}^3 ({P['n_elems']} tets, {en.n_dofs} dofs), "
+                       f"jitter 0.2h, 20% stretch in {steps} load steps, rel-res 1e-10 per step",
+           "seconds": total, "setup_s": setup_s, "newton_iterations": newton_its,
+           "cg_iterations": cg_its, "nnz": cm.nnz, "n_colors": cm.n_colors,
+           "converged_steps": sum(1 for h in hist if h["converged"]),
+           "dof_newton_iterations_per_s": en.n_dofs * newton_its / total, "steps": hist}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = _cpu_newton_sample()
+    return out
+
+
+def _cpu_newton_sample(n=10):
+    import scipy.sparse as sps
+    import scipy.sparse.linalg as spla
+
+    from oracle import elements as oe
+    from oracle import materials as omat
+    from oracle import operator as oop
+    from oracle import sparse as osp
+    from tatva_gb300.problems import stretched_kuhn
+
+    P = stretched_kuhn(n, "cpu")
+    c, e = P["coords"], P["mesh"].elements_host()
+    op = oop.OracleOperator(c, e, oe.Tetrahedron4())
+    law = omat.NeoHookean(1.0, 10.0)
+    pat = osp.pattern_from_mesh(c, e, 3)
+    nd = c.shape[0] * 3
+    dofs = P["dofs"]
+    free = np.setdiff1d(np.arange(nd), dofs)
+    u = np.zeros(nd)
+    u[0::3] = c[:, 0] * 0.02
+    u[dofs] = P["values"](0.02)
+    its, t0 = 0, time.perf_counter()
+    r0 = None
+    for _ in range(30):
+        r = omat.residual(op, law, u)[free]
+        rn = np.linalg.norm(r)
+        r0 = rn if r0 is None else r0
+        if rn <= 1e-10 * r0:
+            break
+        Ke = omat.element_tangents(op, law, u)
+        data = omat.assemble_csr_data(op, Ke, 3, pat.indptr, pat.indices)
+        K = sps.csr_matrix((data, pat.indices, pat.indptr), shape=(nd, nd))[free][:, free]
+        u[free] -= spla.spsolve(K.tocsc(), r)
+        its += 1
+    dt = time.perf_counter() - t0
+    return {"value": nd * its / dt, "unit": "dof-Newton-iterations/s", "cores": 1, "kind": "port",
+            "sample": f"one 2% load step on a Kuhn {n}^3 block ({nd} dofs): {its} Newton "
+                      f"iterations, numpy element tangents + scipy sparse direct solve, {dt:.1f} s"}
+
+
 def run_ours(args):
     import torch
 
     from tatva_gb300 import _lib, autotune, solvers
     from tatva_gb300._device import ptr
 
-    ws, rank, local = _dist()
-    if ws > 1:
-        import torch.distributed as dist
+    from tatva_gb300 import replicas
 
-        dist.init_process_group("nccl")
+    ws, rank, local = replicas.world()
     torch.cuda.set_device(local)
+    replicas.init("nccl")
     dev = torch.device("cuda", local)
     P = brick_problem(args.size, dev)
     en = P["energy"]
@@ -395,12 +480,22 @@ def run_ours(args):
     def hvp_step(vv, out):
         en.apply(_lib.TG_MODE_HVP, None, vv, out=out)
 
+    # the HVP is captured once in a CUDA graph and replayed each step, so that host-side
+    # launch latency of the Python wrapper does not leak into the device time
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(st)
+    with torch.cuda.stream(side):
+        hvp_step(v, y)
+    st.wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        hvp_step(v, y)
     for _ in range(args.warmup):
         flush.fill_(1.0)
-        hvp_step(v, y)
+        graph.replay()
     torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
     with ClockSampler(local) as clk:
@@ -409,18 +504,15 @@ def run_ours(args):
         for i in range(args.steps):
             flush.fill_(float(i))
             evs[i][0].record(st)
-            hvp_step(v, y)
+            graph.replay()
             evs[i][1].record(st)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     clocks = clk.summary()
     ms = [a.elapsed_time(b) for a, b in evs]
-    ms_step = float(np.mean(ms))
-    if ws > 1:
-        t = torch.tensor([ms_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = ws * ndof / (ms_step * 1e-3) / 1e9
+    replicas.barrier()
+    ms_step = replicas.max_over_ranks(float(np.mean(ms)))
+    value = replicas.sum_over_ranks(ndof) / (ms_step * 1e-3) / 1e9
 
     # ---- e2e through the public API with host buffers
     vh = torch.empty(ndof, dtype=torch.float32, pin_memory=True)
@@ -435,8 +527,8 @@ def run_ours(args):
         yh.copy_(en.hvp(None, vh.to(dev, non_blocking=True)), non_blocking=True)
     e.record(st)
     torch.cuda.synchronize()
-    e2e_ms = s.elapsed_time(e) / args.steps
-    e2e_value = ws * ndof / (e2e_ms * 1e-3) / 1e9
+    e2e_ms = replicas.max_over_ranks(s.elapsed_time(e) / args.steps)
+    e2e_value = replicas.sum_over_ranks(ndof) / (e2e_ms * 1e-3) / 1e9
 
     # ---- roofline of the HVP
     nn, ne = P["n_nodes"], P["n_elems"]
@@ -473,8 +565,7 @@ def run_ours(args):
                       "converged": rmx.converged, "message": rmx.message, "solves_per_s": 1.0 / rmx.seconds},
             "speedup_mixed_vs_fp64": r64.seconds / rmx.seconds,
         }
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     if rank != 0:
         return
     cpu = None
@@ -513,6 +604,8 @@ def run_ours(args):
         line["batched"] = bench_batched(dev, args)
     if args.serving:
         line["serving"] = bench_serving(dev, args)
+    if args.newton:
+        line["newton"] = bench_newton(dev, args)
     print(json.dumps(line), flush=True)
 
 
@@ -534,6 +627,8 @@ def main():
     ap.add_argument("--batched", type=int, default=4096, help="meshes in the batched solve (0: skip)")
     ap.add_argument("--serving", type=int, default=200, help="requests in the serving run (0: skip)")
     ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--newton", type=int, default=96, help="Kuhn cells per side (0: skip)")
+    ap.add_argument("--newton-steps", type=int, default=10)
     ap.add_argument("--hbm-budget", type=int, default=32, help="serving HBM budget, GiB")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -206,7 +206,8 @@ TG_API int tg_plan_box_geometry(const tg_block_plan* plan, const float* coords, 
  * Lifter.reduce_adjoint/Fixed (tatva/lifter/base.py:235-251,
  * lifter/constraints.py:312-318): inputs v are read as 0 on fixed dofs and the
  * output on fixed dofs is 0 (RESIDUAL), v (HVP, identity block) or 1 (DIAG).
- * coords must have precision prec.  Workspace: tg_apply_workspace_bytes.     */
+ * coords must have precision prec.  Workspace: tg_apply_workspace_bytes.
+ * Entries of y that belong to nodes no element references are not written.      */
 TG_API size_t tg_apply_workspace_bytes(int elem, int prec, int mat_kind, const tg_block_plan* plan);
 TG_API int tg_apply(int elem, int prec, int mode, const tg_material* mat, const tg_block_plan* plan,
              const void* coords, int64_t n_nodes, const void* u, const void* v,

@@ -110,3 +110,38 @@ class OracleOperator:
         out = np.zeros((n_nodes,) + contrib.shape[2:], dtype=contrib.dtype)
         np.add.at(out, self.elements, contrib)
         return out
+
+
+def project(op: OracleOperator, field, fixed_nodes=None, fixed_values=None):
+    """L2 projection of a quadrature field onto the nodal space, following
+    make_project_function / _make_projection / _solve_projection
+    (tatva/utils.py:118-262): M x = b with the consistent mass matrix
+    M_ab = sum_e int N_a N_b and b_a = int N_a field, solved per field component
+    (the coupled vector system is M (x) I); with a lifter (nodes ``fixed_nodes``)
+    the reduced system M_ff x_f = b_f is solved and the fixed nodes take their
+    prescribed values (Lifter.lift_from_zeros, tatva/lifter/base.py:223-229)."""
+    import scipy.sparse as sps
+    import scipy.sparse.linalg as spla
+
+    field = np.asarray(field, dtype=np.float64)
+    E, Q = field.shape[:2]
+    vshape = field.shape[2:]
+    F = field.reshape(E, Q, -1)
+    nn = op.coords.shape[0]
+    _, detJ = op.geometry()
+    w = detJ * op.qw[None, :]
+    Me = np.einsum("eq,qa,qb->eab", w, op.N, op.N)
+    rows = np.repeat(op.elements, op.elements.shape[1], axis=1).ravel()
+    cols = np.tile(op.elements, (1, op.elements.shape[1])).ravel()
+    M = sps.coo_matrix((Me.ravel(), (rows, cols)), shape=(nn, nn)).tocsr()
+    b = op.eval_transpose(F * w[:, :, None])  # (nn, C)
+    free = np.ones(nn, dtype=bool)
+    if fixed_nodes is not None:
+        free[np.asarray(fixed_nodes)] = False
+    x = np.zeros_like(b)
+    Mf = M[free][:, free].tocsc()
+    for c in range(b.shape[1]):
+        x[free, c] = spla.spsolve(Mf, b[free, c])
+    if fixed_nodes is not None:
+        x[~free] = 0.0 if fixed_values is None else np.asarray(fixed_values).reshape(-1, 1)
+    return x.reshape((nn,) + vshape)

@@ -3,9 +3,9 @@
 // The reference has no solver: users compose jax.scipy.sparse.linalg.cg with the
 // matrix-free HVP (README.md:93).  Here:
 //   * CSR SpMV (layout of ColoredMatrix.to_csr, tatva/sparse/base.py:76-81)
-//   * deterministic FP64 dot products: a fixed partition into DOT_CHUNKS chunks and a
-//     fixed tree order, independent of the GPU and of the launch, so repeated solves
-//     are bitwise identical
+//   * deterministic FP64 dot products: a fixed partition (one chunk per 2048 entries,
+//     at most DOT_CHUNKS chunks) and a fixed tree order, independent of the GPU and of
+//     the launch, so repeated solves are bitwise identical
 //   * Jacobi-preconditioned CG whose scalars never leave the device; `check_every`
 //     iterations are captured once in a CUDA graph and replayed between host
 //     convergence checks; every loop is bounded by max_iter
@@ -74,9 +74,18 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[K], double* __res
   }
 }
 
-// fixed partition into DOT_CHUNKS chunks whose starts are multiples of 4 elements
+// Chunk count of the fixed partition of an n-vector: one chunk per 2048 entries, at
+// most DOT_CHUNKS (small vectors launch few CTAs; the count depends on n only).
+__host__ __device__ inline int dot_chunks(int64_t n) {
+  const int64_t c = (n + 2047) / 2048;
+  return (int)(c < 1 ? 1 : (c > DOT_CHUNKS ? DOT_CHUNKS : c));
+}
+
+// fixed partition into gridDim.x (= dot_chunks(n)) chunks whose starts are multiples
+// of 4 elements
 __device__ __forceinline__ void chunk_range(int64_t n, int64_t& i0, int64_t& i1) {
-  const int64_t chunk = (((n + DOT_CHUNKS - 1) / DOT_CHUNKS) + 3) & ~int64_t(3);
+  const int64_t nc = gridDim.x;
+  const int64_t chunk = (((n + nc - 1) / nc) + 3) & ~int64_t(3);
   i0 = min(n, (int64_t)blockIdx.x * chunk);
   i1 = min(n, i0 + chunk);
 }
@@ -119,14 +128,14 @@ __global__ void __launch_bounds__(DOT_THREADS)
   block_reduce_store<1>(v, part + blockIdx.x);
 }
 
-// sums DOT_CHUNKS partials (stride K) into out[k]
+// sums nchunks partials (stride K) into out[k]
 template <int K>
 __global__ void __launch_bounds__(DOT_THREADS)
-    dot_final_kernel(const double* __restrict__ part, double* __restrict__ out) {
+    dot_final_kernel(const double* __restrict__ part, double* __restrict__ out, int nchunks) {
   double v[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) v[k] = 0.0;
-  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS)
+  for (int b = threadIdx.x; b < nchunks; b += DOT_THREADS)
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] += part[b * K + k];
   block_reduce_store<K>(v, out);
@@ -147,19 +156,32 @@ __global__ void convert_kernel(const Ti* __restrict__ in, To* __restrict__ out, 
 }
 
 // ------------------------------------------------------------------ CSR
+// SPMV_LANES lanes per row (4 rows per warp): the finite-element rows here hold 7 to
+// 81 entries, for which a whole warp per row leaves most lanes idle.  Fixed lane
+// count and reduction tree: the result does not depend on the launch.
+constexpr int SPMV_LANES = 8;
 template <class T>
 __global__ void spmv_kernel(int64_t n_rows, const int32_t* __restrict__ indptr,
                             const int32_t* __restrict__ indices, const T* __restrict__ data,
                             const T* __restrict__ x, T* __restrict__ y) {
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-  const int lane = threadIdx.x & 31;
-  if (row >= n_rows) return;
-  const int k0 = __ldg(indptr + row), k1 = __ldg(indptr + row + 1);
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / SPMV_LANES;
+  const int lane = threadIdx.x & (SPMV_LANES - 1);
+  const bool live = row < n_rows;
   T acc = T(0);
-  for (int k = k0 + lane; k < k1; k += 32) acc += __ldg(data + k) * x[__ldg(indices + k)];
+  if (live) {
+    const int k0 = __ldg(indptr + row), k1 = __ldg(indptr + row + 1);
+    int k = k0 + lane;
+    for (; k + SPMV_LANES < k1; k += 2 * SPMV_LANES) {
+      const T a0 = __ldg(data + k), a1 = __ldg(data + k + SPMV_LANES);
+      const T x0 = x[__ldg(indices + k)], x1 = x[__ldg(indices + k + SPMV_LANES)];
+      acc += a0 * x0;
+      acc += a1 * x1;
+    }
+    if (k < k1) acc += __ldg(data + k) * x[__ldg(indices + k)];
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) y[row] = acc;
+  for (int o = SPMV_LANES / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, SPMV_LANES);
+  if (live && lane == 0) y[row] = acc;
 }
 
 template <class T>
@@ -225,9 +247,10 @@ __global__ void __launch_bounds__(DOT_THREADS)
 }
 
 // scal[RZ] = rz, scal[RR] = rr from the two-slot partials
-__global__ void cg_init_final_kernel(const double* __restrict__ part, double* __restrict__ scal) {
+__global__ void cg_init_final_kernel(const double* __restrict__ part, double* __restrict__ scal,
+                                     int nchunks) {
   double v[2] = {0.0, 0.0};
-  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS) {
+  for (int b = threadIdx.x; b < nchunks; b += DOT_THREADS) {
     v[0] += part[2 * b];
     v[1] += part[2 * b + 1];
   }
@@ -242,9 +265,10 @@ __global__ void cg_init_final_kernel(const double* __restrict__ part, double* __
 }
 
 // alpha = rz / pq (breakdown flag on pq <= 0 or non-finite)
-__global__ void cg_alpha_kernel(const double* __restrict__ part, double* __restrict__ scal) {
+__global__ void cg_alpha_kernel(const double* __restrict__ part, double* __restrict__ scal,
+                                int nchunks) {
   double v[1] = {0.0};
-  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS) v[0] += part[b];
+  for (int b = threadIdx.x; b < nchunks; b += DOT_THREADS) v[0] += part[b];
   __shared__ double out[1];
   block_reduce_store<1>(v, out);
   __syncthreads();
@@ -302,9 +326,10 @@ __global__ void __launch_bounds__(DOT_THREADS)
 }
 
 // beta = rz_new / rz; rz = rz_new; rr stored
-__global__ void cg_beta_kernel(const double* __restrict__ part, double* __restrict__ scal) {
+__global__ void cg_beta_kernel(const double* __restrict__ part, double* __restrict__ scal,
+                               int nchunks) {
   double v[2] = {0.0, 0.0};
-  for (int b = threadIdx.x; b < DOT_CHUNKS; b += DOT_THREADS) {
+  for (int b = threadIdx.x; b < nchunks; b += DOT_THREADS) {
     v[0] += part[2 * b];
     v[1] += part[2 * b + 1];
   }
@@ -391,7 +416,7 @@ extern "C" int tg_spmv(int prec, int64_t n_rows, const int32_t* indptr, const in
   TG_TRY(check_ptr(y, "y"));
   return dispatch_prec(prec, [&](auto t) -> int {
     using T = decltype(t);
-    spmv_kernel<T><<<grid_for(n_rows * 32, 256), 256, 0, as_stream(stream)>>>(
+    spmv_kernel<T><<<grid_for(n_rows * SPMV_LANES, 256), 256, 0, as_stream(stream)>>>(
         n_rows, indptr, indices, (const T*)data, (const T*)x, (T*)y);
     return launch_check("tg_spmv");
   });
@@ -434,9 +459,9 @@ extern "C" int tg_dot(int prec, const void* x, const void* y, int64_t n, double*
   cudaStream_t st = as_stream(stream);
   return dispatch_prec(prec, [&](auto t) -> int {
     using T = decltype(t);
-    dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>((const T*)x, (const T*)y, n,
+    dot_partial_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)x, (const T*)y, n,
                                                               (double*)workspace);
-    dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>((const double*)workspace, out_dev);
+    dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>((const double*)workspace, out_dev, dot_chunks(n));
     return launch_check("tg_dot");
   });
 }
@@ -521,9 +546,9 @@ static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* 
   const int64_t n = op_ndofs(op);
   TG_TRY(tg_operator_apply(op, x, B.r, B.apply_ws, B.apply_bytes, st));
   axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
-  cg_init_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(n, (const T*)B.r, diag, (T*)B.z,
+  cg_init_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, (const T*)B.r, diag, (T*)B.z,
                                                         (T*)B.p, B.part);
-  cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal);
+  cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
   return launch_check("cg restart");
 }
 
@@ -532,13 +557,13 @@ static int cg_iteration(const tg_operator_desc* op, T* x, const T* diag, CgBuffe
                         cudaStream_t st) {
   const int64_t n = op_ndofs(op);
   TG_TRY(tg_operator_apply(op, B.p, B.q, B.apply_ws, B.apply_bytes, st));
-  dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n,
+  dot_partial_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n,
                                                             B.part);
-  cg_alpha_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal);
-  cg_update_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(n, B.scal, x, (T*)B.r, (T*)B.z,
+  cg_alpha_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
+  cg_update_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, B.scal, x, (T*)B.r, (T*)B.z,
                                                           (const T*)B.p, (const T*)B.q, diag,
                                                           B.part);
-  cg_beta_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal);
+  cg_beta_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
   cg_p_kernel<T><<<grid_for((n + 3) / 4, 256), 256, 0, st>>>(n, B.scal, (const T*)B.z, (T*)B.p);
   return launch_check("cg iteration");
 }
@@ -612,10 +637,10 @@ static int true_residual_norm(const tg_operator_desc* op, const T* bvec, const T
   const int64_t n = op_ndofs(op);
   TG_TRY(tg_operator_apply(op, x, B.r, B.apply_ws, B.apply_bytes, st));
   axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
-  dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>((const T*)B.r, (const T*)B.r, n, B.part);
-  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(B.part, B.scal + 5);
-  dot_partial_kernel<T><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(bvec, bvec, n, B.part);
-  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(B.part, B.scal + 7);
+  dot_partial_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)B.r, (const T*)B.r, n, B.part);
+  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(B.part, B.scal + 5, dot_chunks(n));
+  dot_partial_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(bvec, bvec, n, B.part);
+  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(B.part, B.scal + 7, dot_chunks(n));
   TG_TRY(launch_check("true residual"));
   double h[SCAL_N];
   TG_TRY(read_scalars(B.scal, h, st));
@@ -708,8 +733,8 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
 
   convert_kernel<double, float><<<grid_for(n, 256), 256, 0, st>>>(diag64, diag32, n);
   // |b|^2
-  dot_partial_kernel<double><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(b, b, n, part);
-  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(part, sc + 1);
+  dot_partial_kernel<double><<<dot_chunks(n), DOT_THREADS, 0, st>>>(b, b, n, part);
+  dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(part, sc + 1, dot_chunks(n));
   TG_TRY(launch_check("mixed: setup"));
   int total_inner = 0, outer = 0, rc = TG_OK;
   double rn = 0.0, bn = 0.0;
@@ -718,8 +743,8 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
     // true residual r64 = b - A64 x in FP64
     TG_TRY(tg_operator_apply(op64, x, r64, aws64, ab64, st));
     axpby_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, b, -1.0, r64);
-    dot_partial_kernel<double><<<DOT_CHUNKS, DOT_THREADS, 0, st>>>(r64, r64, n, part);
-    dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(part, sc);
+    dot_partial_kernel<double><<<dot_chunks(n), DOT_THREADS, 0, st>>>(r64, r64, n, part);
+    dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(part, sc, dot_chunks(n));
     TG_TRY(launch_check("mixed: residual"));
     TG_TRY(cuda_check(cudaMemcpyAsync(h, sc, 8 * sizeof(double), cudaMemcpyDeviceToHost, st), "mixed: read"));
     TG_TRY(cuda_check(cudaStreamSynchronize(st), "mixed: sync"));

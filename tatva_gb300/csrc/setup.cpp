@@ -654,13 +654,14 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
     P->color_ofs.reserve(P->blk_color_ptr[nb]);
     for (int32_t b = 0; b < nb; ++b)
       P->color_ofs.insert(P->color_ofs.end(), blk_colors[b].begin(), blk_colors[b].end());
-    // 4. partial slots in (block, local node) order, then node -> slots CSR
+    // 4. partial slots: the slots of one shared node are consecutive (its blocks in
+    // block order), so the final sum over a node reads one contiguous run
     int64_t slot = 0;
     std::vector<int32_t> nshare(n_nodes, 0);
     for (int32_t b = 0; b < nb; ++b)
       for (int32_t l = P->blk_node_ptr[b]; l < P->blk_node_ptr[b + 1]; ++l)
         if (P->lnode_slot[l] == -2) {
-          P->lnode_slot[l] = (int32_t)slot++;
+          ++slot;
           nshare[P->lnode_gid[l]]++;
         }
     if (slot > INT32_MAX) {
@@ -676,11 +677,12 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
     const int64_t nsh = (int64_t)P->shared_node.size();
     P->shared_ptr.assign(nsh + 1, 0);
     for (int64_t s = 0; s < nsh; ++s) P->shared_ptr[s + 1] = P->shared_ptr[s] + nshare[P->shared_node[s]];
-    P->shared_slots.assign(slot, 0);
+    P->shared_slots.resize(slot);
+    for (int64_t k = 0; k < slot; ++k) P->shared_slots[k] = (int32_t)k;
     std::vector<int32_t> fill(P->shared_ptr.begin(), P->shared_ptr.end() - 1);
     for (int32_t b = 0; b < nb; ++b)
       for (int32_t l = P->blk_node_ptr[b]; l < P->blk_node_ptr[b + 1]; ++l)
-        if (P->lnode_slot[l] >= 0) P->shared_slots[fill[sidx[P->lnode_gid[l]]]++] = P->lnode_slot[l];
+        if (P->lnode_slot[l] == -2) P->lnode_slot[l] = fill[sidx[P->lnode_gid[l]]]++;
     *handle = P;
   } catch (const std::bad_alloc&) {
     return set_error(TG_ERR_VALUE, "tg_plan_build: out of host memory");

@@ -131,6 +131,19 @@ class Energy:
         _lib.call("tg_apply", self.op.element.tg_id, prec, mode, ctypes.byref(m), plan.ref(),
                   ptr(self.op.coords_as(dtype)), self.op.n_nodes, ptr(uf), ptr(vf), ptr(mask),
                   ptr(y), ptr(ws), nb, stream())
+        orphans = self.op.unused_nodes()
+        if orphans.numel():
+            # rows of nodes without elements: zero, with the Dirichlet rule on fixed dofs
+            nv = self.n_values
+            dofs = (orphans[:, None] * nv + torch.arange(nv, device=y.device)).reshape(-1)
+            val = torch.zeros(dofs.numel(), dtype=y.dtype, device=y.device)
+            if mask is not None:
+                fx = mask[dofs].bool()
+                if mode == _lib.TG_MODE_HVP:
+                    val = torch.where(fx, vf[dofs], val)
+                elif mode == _lib.TG_MODE_DIAG:
+                    val = torch.where(fx, torch.ones_like(val), val)
+            y[dofs] = val
         return y.view(ref.shape) if out is None else y
 
     # ------------------------------------------------------------------ public API

@@ -30,6 +30,8 @@ Validation follows ``Operator.__check_init__`` (:132-170): ``ValueError`` /
 
 from __future__ import annotations
 
+import dataclasses
+
 import math
 from numbers import Number
 from typing import Callable, Sequence
@@ -145,6 +147,16 @@ class Operator:
                                          block_elems=block_elems,
                                          max_local_nodes=max_local_nodes or DEFAULT_MAX_LOCAL,
                                          threads=threads or 256)
+        return self._cache[key]
+
+    def unused_nodes(self) -> torch.Tensor:
+        """Nodes that no element references (cached); the fused kernels do not write
+        their entries."""
+        key = "unused_nodes"
+        if key not in self._cache:
+            used = np.zeros(self.n_nodes, dtype=bool)
+            used[self.mesh.elements_host().reshape(-1)] = True
+            self._cache[key] = torch.as_tensor(np.where(~used)[0], device=self.device)
         return self._cache[key]
 
     def _nodal_shape(self, u: torch.Tensor):
@@ -337,8 +349,59 @@ class Operator:
         raise NotImplementedError(
             "Operator.interpolate (point location) is not part of the GB300 hot path")
 
-    def project(self, field, colored_matrix=None, lifter=None):
-        raise NotImplementedError("Operator.project is not part of the GB300 hot path")
+    def project(self, field: torch.Tensor, colored_matrix=None, lifter=None,
+                rtol: float = 1e-13) -> torch.Tensor:
+        """L2 projection of a quadrature field (E, Q, ...) onto the nodes
+        (operator.py:523-554, tatva/utils.py:118-262): M x = b with the consistent mass
+        matrix M_ab = int N_a N_b, assembled on the scalar pattern by the colored
+        Jacobian kernels (one mass-operator application per colour), and
+        b_a = int N_a field, solved per component by device CG to ``rtol`` (the
+        reference uses a sparse direct solve).  With a ``lifter`` (scalar dofs = nodes)
+        the reduced system is solved and constrained nodes take the lifter's values
+        (Lifter.lift_from_zeros)."""
+        from . import sparse, solvers
+
+        require_cuda(field)
+        f = field.to(torch.float64).contiguous()
+        if f.ndim < 2 or f.shape[0] != self.n_elements or f.shape[1] != self.n_quad:
+            raise ValueError(f"field must be shaped (n_elements={self.n_elements}, "
+                             f"n_quad={self.n_quad}, ...), got {tuple(field.shape)}")
+        nn = self.n_nodes
+        if colored_matrix is not None and colored_matrix.shape[0] % nn:
+            raise ValueError("colored matrix size is not a multiple of the number of nodes")
+        if lifter is not None and lifter.size != nn:
+            raise NotImplementedError("projection with a lifter needs one dof per node")
+        vshape = tuple(f.shape[2:])
+        F = f.reshape(self.n_elements, self.n_quad, -1)
+        key = "proj_mass"
+        if key not in self._cache:
+            cm = sparse.ColoredMatrix.from_csr(sparse.pattern_from_mesh(self.mesh, 1),
+                                               device=self.device)
+            w = self._weights(torch.float64)
+
+            def mass(u):
+                return self._eval_t_raw((self._eval_raw(u.contiguous()) * w).contiguous(), ())
+
+            Jc = torch.empty((nn, cm.n_colors), dtype=torch.float64, device=self.device)
+            for c in range(cm.n_colors):
+                Jc[:, c] = mass((cm.colors == c).to(torch.float64))
+            rows, cols = sparse.compute_rows_cols(cm)
+            M = dataclasses.replace(cm, data=sparse.decompress(Jc, rows, cols))
+            self._cache[key] = M
+        M = self._cache[key]
+        w = self._weights(torch.float64)
+        mask = lifter.fixed_mask(self.device) if lifter is not None else None
+        out = torch.empty((nn, F.shape[2]), dtype=torch.float64, device=self.device)
+        for c in range(F.shape[2]):
+            b = self._eval_t_raw((F[:, :, c] * w).contiguous(), ())
+            if mask is not None:
+                b = torch.where(mask.bool(), torch.zeros_like(b), b)
+            r = solvers.csr_cg(M, b, fixed=mask, rtol=rtol, maxiter=10000, check_every=10)
+            out[:, c] = r.x
+        if lifter is not None:
+            for k in range(F.shape[2]):
+                out[:, k] = lifter.lift(lifter.reduce(out[:, k]), out[:, k])
+        return out.reshape((nn,) + vshape)
 
     def _replace(self, **changes):
         kw = dict(mesh=self.mesh, element=self.element, batch_size=self.batch_size,

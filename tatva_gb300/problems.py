@@ -40,4 +40,35 @@ def clamped_brick(n: int, device, traction: float = 1e-3, young: float = 1.0,
                 b=torch.as_tensor(b, device=device), n_nodes=nn, n_elems=mesh.n_elements)
 
 
-__all__ = ["clamped_brick"]
+
+
+def stretched_kuhn(n: int, device, jitter: float = 0.2, seed: int = 0, mu: float = 1.0,
+                   lmbda: float = 10.0) -> dict:
+    """Neo-Hookean Tet4 block: Kuhn 6-tet split of [0,1]^3 with n^3 cells (the node
+    and tet order of the reference's Kuhn-box fixture, tests/test_sparse_tracer.py:29-70),
+    interior nodes displaced by U(+-jitter h) from numpy default_rng(seed); the faces
+    x = 0 and x = 1 are held, x = 1 moved along x by the prescribed stretch."""
+    from .element import Tetrahedron4
+    from .materials import NeoHookean
+    from .mesh import jitter_interior
+
+    m0 = Mesh.kuhn_box(n, n, n, device="cpu")
+    c = jitter_interior(m0.coords_host(), 1.0 / n, jitter, seed=seed) if jitter else m0.coords_host()
+    mesh = Mesh(c, m0.elements_host(), device=device)
+    op = Operator(mesh, Tetrahedron4())
+    en = NeoHookean(op, mu, lmbda)
+    left = np.where(c[:, 0] == 0.0)[0]
+    right = np.where(c[:, 0] == 1.0)[0]
+    dofs = np.concatenate([left * 3, left * 3 + 1, left * 3 + 2,
+                           right * 3, right * 3 + 1, right * 3 + 2])
+
+    def values(stretch: float) -> np.ndarray:
+        v = np.zeros(len(dofs))
+        v[3 * len(left): 4 * len(left)] = stretch
+        return v
+
+    return dict(mesh=mesh, op=op, energy=en, coords=c, dofs=dofs, values=values,
+                n_nodes=c.shape[0], n_elems=mesh.n_elements)
+
+
+__all__ = ["clamped_brick", "stretched_kuhn"]

@@ -169,10 +169,16 @@ def csr_cg(cm, b: torch.Tensor, x0=None, *, fixed=None, rtol: float = 1e-8,
 
 
 def newton(energy, u0: torch.Tensor, lifter, *, colored_matrix=None, rtol: float = 1e-10,
-           max_iter: int = 25, tangent_dtype=torch.float32, cg_rtol: float = 1e-6,
+           max_iter: int = 25, tangent_dtype=torch.float32, cg_rtol: float | None = None,
+           forcing: str = "adaptive", eta_max: float = 1e-2,
            external_force: torch.Tensor | None = None) -> SolveResult:
     """Newton for min E(u) - f.u with Dirichlet values from ``lifter`` (FP64 residual and
     update; colored sparse tangent in ``tangent_dtype``; CSR CG inner solve).
+
+    Inner tolerance: ``forcing="fixed"`` solves every step to ``cg_rtol`` (default 1e-6);
+    ``"adaptive"`` uses the Eisenstat-Walker rule eta_k = 0.9 (|F_k| / |F_{k-1}|)^2
+    (safeguarded, at most ``eta_max``), never tighter than needed for the final
+    tolerance nor than 10 machine epsilons of the tangent precision.
 
     ``u0`` must already carry the prescribed values on the constrained dofs."""
     from . import sparse
@@ -190,6 +196,10 @@ def newton(energy, u0: torch.Tensor, lifter, *, colored_matrix=None, rtol: float
     status = _lib.TG_ERR_NOT_CONVERGED
     it = 0
     total_cg = 0
+    if forcing not in ("fixed", "adaptive"):
+        raise ValueError("forcing must be 'fixed' or 'adaptive'")
+    eta_floor = 10.0 * float(torch.finfo(tangent_dtype).eps)
+    eta_prev, rn_prev = None, None
     for it in range(max_iter + 1):
         r = energy.residual(u, fixed=mask)
         if fext is not None:
@@ -203,8 +213,21 @@ def newton(energy, u0: torch.Tensor, lifter, *, colored_matrix=None, rtol: float
             break
         if it == max_iter:
             break
+        if forcing == "fixed":
+            eta = 1e-6 if cg_rtol is None else cg_rtol
+        else:
+            if rn_prev is None:
+                eta = eta_max
+            else:
+                eta = 0.9 * (rn / rn_prev) ** 2
+                guard = 0.9 * eta_prev ** 2
+                if guard > 0.1:
+                    eta = max(eta, guard)
+                eta = min(eta, eta_max)
+            eta = max(eta, 0.5 * rtol * max(ref, 1e-300) / rn, eta_floor)
+        eta_prev, rn_prev = eta, rn
         K = jac(u.to(tangent_dtype))
-        sol = csr_cg(K, -r, fixed=mask, rtol=cg_rtol, raise_on_fail=False)
+        sol = csr_cg(K, -r, fixed=mask, rtol=eta, raise_on_fail=False)
         total_cg += sol.iterations
         if sol.status == _lib.TG_ERR_BREAKDOWN or not bool(torch.isfinite(sol.x).all()):
             status = _lib.TG_ERR_BREAKDOWN  # indefinite tangent: stop, keep the last iterate

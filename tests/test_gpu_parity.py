@@ -346,3 +346,49 @@ def test_colored_hessian_neo_hookean(golden, cuda, key, dtype):
     Jc = np.stack([Kd[:, colors == c].sum(1) for c in range(colors.max() + 1)], 1)
     Jc_gpu = en.compressed_hessian(_t(u, cuda, dtype), cm.colors, cm.n_colors)
     assert rel(Jc_gpu, Jc) < (F64_TOL if dtype == torch.float64 else 1e-4)
+
+
+@pytest.mark.parametrize("key", ["hexj", "hexa"])
+def test_operator_project_matches_oracle(golden, cuda, key):
+    """Operator.project (operator.py:523-554, utils.py:118-262): scalar and vector
+    quadrature fields, with and without a lifter, vs the oracle's direct solve."""
+    from oracle.operator import project as oproject
+    from tatva_gb300.lifter import Fixed, Lifter
+
+    c, e = golden[f"{key}_coords"], golden[f"{key}_elements"]
+    op = Operator(Mesh(c, e, device=cuda), ELS[MESHES[key]][0]())
+    oo = oop.OracleOperator(c, e, ELS[MESHES[key]][1]())
+    xq = op.eval(torch.as_tensor(c, device=cuda))  # (E, Q, D) physical QP coordinates
+    fs = torch.sin(3 * xq[..., 0]) + xq[..., 1] ** 2
+    fv = torch.stack([fs, xq[..., 0] * xq[..., 1]], dim=-1)
+    for field in (fs, fv):
+        got = op.project(field)
+        want = oproject(oo, field.cpu().numpy())
+        assert rel(got, want) < 1e-10
+    bnd = np.where(np.isclose(c[:, 0], c[:, 0].min()))[0]
+    lifter = Lifter(c.shape[0], Fixed(bnd, 0.5))
+    got = op.project(fs, lifter=lifter)
+    want = oproject(oo, fs.cpu().numpy(), fixed_nodes=bnd, fixed_values=np.full(len(bnd), 0.5))
+    assert rel(got, want) < 1e-10
+
+
+def test_nodes_without_elements(cuda):
+    """Ragged input: a mesh whose node list holds nodes that no element uses (the
+    reference's gradient is zero there)."""
+    c, e = om.brick(3, 2, 2)
+    c = np.vstack([c, [[5.0, 5.0, 5.0], [6.0, 5.0, 5.0]]])  # two unused nodes at the end
+    op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    oo = oop.OracleOperator(c, e, oe.Hexahedron8())
+    en, law = materials.LinearElastic(op, 0.7, 1.9), omat.LinearElastic(0.7, 1.9)
+    rng = np.random.default_rng(3)
+    u, v = 0.01 * rng.standard_normal(c.shape[0] * 3), rng.standard_normal(c.shape[0] * 3)
+    for dt, tol in ((torch.float64, F64_TOL), (torch.float32, 1e-5)):
+        r = en.residual(_t(u, cuda, dt))
+        h = en.hvp(None, _t(v, cuda, dt))
+        assert rel(r, omat.residual(oo, law, u)) < tol
+        assert rel(h, omat.hvp(oo, law, u, v)) < tol
+        assert torch.count_nonzero(r[-6:]) == 0 and torch.count_nonzero(h[-6:]) == 0
+    fixed = torch.zeros(c.shape[0] * 3, dtype=torch.uint8, device=cuda)
+    fixed[-3:] = 1
+    h = en.hvp(None, _t(v, cuda), fixed=fixed)
+    assert torch.equal(h[-3:], _t(v, cuda)[-3:]) and torch.count_nonzero(h[-6:-3]) == 0

@@ -194,3 +194,21 @@ def test_lifter_known_answers():
     np.testing.assert_array_equal(lf.reduce_adjoint(np.arange(6.0)), [1, 2, 3, 4])
     lf2 = olift.Lifter(6, olift.Fixed(np.array([0, 5]), np.array([0.0, 1.0])))
     np.testing.assert_array_equal(lf2.lift_from_zeros(np.zeros(4)), [0, 0, 0, 0, 0, 1])
+
+
+@pytest.mark.parametrize("key", ["hexj", "hexa"])
+def test_oracle_projection_reproduces_fe_fields(golden, key):
+    """The L2 projection of the quadrature values of a nodal field is that field
+    (utils.py:118-262 solves M x = int N field).  Hex8's 2x2x2 Gauss rule integrates
+    the mass matrix exactly; the one-point rules of Tri3/Tet4 give a rank-deficient
+    element mass matrix, for which the property does not hold."""
+    from oracle import elements as oe
+    from oracle import operator as oop
+
+    c, e = golden[f"{key}_coords"], golden[f"{key}_elements"]
+    el = oe.Hexahedron8()
+    oo = oop.OracleOperator(c, e, el)
+    rng = np.random.default_rng(1)
+    u = rng.standard_normal((c.shape[0], 2))
+    x = oop.project(oo, oo.eval(u))
+    np.testing.assert_allclose(x, u, rtol=0, atol=1e-11 * np.abs(u).max())

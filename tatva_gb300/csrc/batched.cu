@@ -26,6 +26,7 @@ namespace tg {
 namespace {
 
 constexpr int BATCH_MAX_ROWS = 49152;  // shared-memory p: 192 KB
+constexpr int RU = 4;                  // rows per thread in flight in the CG passes
 
 struct BatchArgs {
   tg_batch_desc d;
@@ -163,15 +164,36 @@ __device__ void solve_system(const BatchArgs& a, int sys, float* p, double* red,
       const double stop = a.inner_rtol * a.inner_rtol * rr0;
       bool broke = false;
       for (int it = 0; it < a.max_inner; ++it) {
+        // rows i0, i0 + NT, ..., i0 + (RU-1) NT together: their loads are independent,
+        // so RU rows' worth of L2 requests are in flight at once.  Accumulation order
+        // (rows in increasing i per thread, entries in increasing k) is unchanged.
         Acc2 pq_acc;
-        for (int i = tid; i < n; i += NT) {
-          float s = 0.f;
+        for (int i0 = tid; i0 < n; i0 += RU * NT) {
+          float sv[RU];
+#pragma unroll
+          for (int u = 0; u < RU; ++u) sv[u] = 0.f;
           for (int k = 0; k < W; ++k) {
-            const int64_t e = (int64_t)k * n + i;
-            s = fmaf(v32[e], p[col[e]], s);
+            float av[RU];
+            uint16_t cv[RU];
+#pragma unroll
+            for (int u = 0; u < RU; ++u) {
+              const int i = i0 + u * NT;
+              const int64_t e = (int64_t)k * n + (i < n ? i : 0);
+              av[u] = v32[e];
+              cv[u] = col[e];
+            }
+#pragma unroll
+            for (int u = 0; u < RU; ++u)
+              if (i0 + u * NT < n) sv[u] = fmaf(av[u], p[cv[u]], sv[u]);
           }
-          q[i] = s;
-          pq_acc.add(p[i], s);
+#pragma unroll
+          for (int u = 0; u < RU; ++u) {
+            const int i = i0 + u * NT;
+            if (i < n) {
+              q[i] = sv[u];
+              pq_acc.add(p[i], sv[u]);
+            }
+          }
         }
         double t1[1] = {pq_acc.value()};
         block_sum<NT, 1>(t1, red, flip);
@@ -180,14 +202,28 @@ __device__ void solve_system(const BatchArgs& a, int sys, float* p, double* red,
         if (!(pq > 0.0) || !isfinite(pq)) { broke = true; break; }
         const float alpha = (float)(rz / pq);
         Acc2 rz2, rr2;
-        for (int i = tid; i < n; i += NT) {
-          const float pi = p[i];
-          dv[i] = fmaf(alpha, pi, dv[i]);
-          const float ri = fmaf(-alpha, q[i], r[i]);
-          r[i] = ri;
-          const float zi = ri * idg[i];
-          rz2.add(ri, zi);
-          rr2.add(ri, ri);
+        for (int i0 = tid; i0 < n; i0 += RU * NT) {
+          float dvv[RU], qv[RU], rv[RU], gv[RU];
+#pragma unroll
+          for (int u = 0; u < RU; ++u) {
+            const int i = i0 + u * NT < n ? i0 + u * NT : i0;
+            dvv[u] = dv[i];
+            qv[u] = q[i];
+            rv[u] = r[i];
+            gv[u] = idg[i];
+          }
+#pragma unroll
+          for (int u = 0; u < RU; ++u) {
+            const int i = i0 + u * NT;
+            if (i < n) {
+              dv[i] = fmaf(alpha, p[i], dvv[u]);
+              const float ri = fmaf(-alpha, qv[u], rv[u]);
+              r[i] = ri;
+              const float zi = ri * gv[u];
+              rz2.add(ri, zi);
+              rr2.add(ri, ri);
+            }
+          }
         }
         double t3[2] = {rz2.value(), rr2.value()};
         block_sum<NT, 2>(t3, red, flip);
@@ -195,6 +231,7 @@ __device__ void solve_system(const BatchArgs& a, int sys, float* p, double* red,
         if (t3[1] <= stop) break;
         const float beta = (float)(t3[0] / rz);
         rz = t3[0];
+#pragma unroll 4
         for (int i = tid; i < n; i += NT) p[i] = fmaf(beta, p[i], r[i] * idg[i]);
         __syncthreads();
       }

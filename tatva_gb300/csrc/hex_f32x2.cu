@@ -256,18 +256,13 @@ __host__ __device__ constexpr int p6_buf_words(int kind) { return kind == P6_BOX
 __host__ __device__ constexpr int p6_smem_words_per_slot(int kind) {
   return 2 * p6_buf_words(kind) + 8;
 }
-__host__ __device__ constexpr int p6_smem_words_fixed(int kind) {
-  return 2 * P6_CRING + (kind == P6_BOX_GEOM ? 3 * P6_MAX_ELEMS : 0);
-}
 
 // shared-memory layout (32-bit words), nl8 = node slots (multiple of 8), B = buffer
 // words per slot (8: X | W, 4: W only):
 //   data buffer s (s = 0, 1) at s * B nl8: [X (4 nl8)] | W (4 nl8)
 //   node-id ring r (r = 0, 1) at 2B nl8 + r nl8, slot ring r at (2B + 2) nl8 + r nl8
 //   Y at (2B + 4) nl8 (4 nl8)
-//   colour-offset ring r at (2B + 8) nl8 + r P6_CRING
-//   box kernel with plan edge terms: [3][P6_MAX_ELEMS] edge terms of the current block
-//   after the colour ring                 total (2B + 8) nl8 + 2 P6_CRING [+ 3 P6_MAX_ELEMS]
+//   colour-offset ring r at (2B + 8) nl8 + r P6_CRING     total (2B + 8) nl8 + 2 P6_CRING
 template <int MODE, int KIND>
 __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
     hex_le_f32x2_kernel(const tg_block_plan p, int b_begin, int b_end,
@@ -283,7 +278,6 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
   int* const qring = reinterpret_cast<int*>(sm + (2 * BW + 2) * nl8);
   float* const Ybuf = sm + (2 * BW + 4) * nl8;
   int* const cring = reinterpret_cast<int*>(sm + (2 * BW + 8) * nl8);
-  float* const gsm = sm + (2 * BW + 8) * nl8 + 2 * P6_CRING;  // GEO only
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   constexpr int NT = P6_THREADS;
@@ -309,18 +303,6 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
       if (l < nl) {
         cp_async4(ring + r * nl8 + l, p.lnode_gid + n0 + l);
         cp_async4(qring + r * nl8 + l, p.lnode_smem + n0 + l);
-      }
-    }
-  };
-  // edge terms of block b's element positions into gsm (GEO only; one buffer: issued
-  // once every read of the previous block's terms is behind a barrier)
-  auto issue_geom = [&](int b) {
-    if constexpr (GEO) {
-      const int e0 = __ldg(p.blk_elem_ptr + b), ne = __ldg(p.blk_elem_ptr + b + 1) - e0;
-      const int64_t ng = p.n_elems;
-      for (int l = tid; l < ne; l += NT) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) cp_async4(gsm + d * P6_MAX_ELEMS + l, p.box_geom32 + d * ng + e0 + l);
       }
     }
   };
@@ -361,7 +343,6 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
   int bi = blockIdx.x;
   if (bi < nblk) issue_ids(b_begin + bi, 0);
   if (bi < nblk) issue_cofs(b_begin + bi, 0);
-  if (bi < nblk) issue_geom(b_begin + bi);
   cp_async_commit();
   cp_async_wait0();
   __syncthreads();
@@ -394,6 +375,7 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
 
     const float* X = sm + s * BW * nl8;
     float* W = const_cast<float*>(X) + (BW - 4) * nl8;
+    const int e_blk = __ldg(p.blk_elem_ptr + b);
     if (MODE == TG_MODE_HVP && fixed) {
 #pragma unroll
       for (int k = 0; k < P6_NPT; ++k) {
@@ -423,10 +405,12 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
       if (actA) {
         f2 R[3][3], detJm;
         if constexpr (GEO) {
-          const int iB = actB ? kB : kA;
-          const float jA0 = gsm[kA], jB0 = gsm[iB];
-          const float jA1 = gsm[P6_MAX_ELEMS + kA], jB1 = gsm[P6_MAX_ELEMS + iB];
-          const float jA2 = gsm[2 * P6_MAX_ELEMS + kA], jB2 = gsm[2 * P6_MAX_ELEMS + iB];
+          const float* gp = p.box_geom32;
+          const int64_t ng = p.n_elems;
+          const int64_t iA = e_blk + kA, iB = e_blk + (actB ? kB : kA);
+          const float jA0 = __ldg(gp + iA), jB0 = __ldg(gp + iB);
+          const float jA1 = __ldg(gp + ng + iA), jB1 = __ldg(gp + ng + iB);
+          const float jA2 = __ldg(gp + 2 * ng + iA), jB2 = __ldg(gp + 2 * ng + iB);
 #pragma unroll
           for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -510,8 +494,6 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
       }
     }
     if (bi + stride < nblk) load_lconn4(b + stride, LC);
-    // every thread is past the colour passes (barriers), so past its reads of gsm
-    if (bi + stride < nblk) issue_geom(b + stride);
 
     // write back this block and clear the accumulator
 #pragma unroll
@@ -578,7 +560,7 @@ static int launch6(const tg_block_plan* plan, int b0, int b1, const float* coord
   if (b1 <= b0) return TG_OK;
   auto k = hex_le_f32x2_kernel<MODE, KIND>;
   const size_t smem =
-      ((size_t)p6_smem_words_per_slot(KIND) * nl8 + p6_smem_words_fixed(KIND)) * sizeof(float);
+      ((size_t)p6_smem_words_per_slot(KIND) * nl8 + 2 * P6_CRING) * sizeof(float);
   int sms = 0, per_sm = 0;
   TG_TRY(launch_shape((const void*)k, smem, sms, per_sm));
   if (per_sm <= 0) return TG_ERR_UNSUPPORTED;
@@ -616,8 +598,7 @@ int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords
   // the general kernel needs the most shared memory: check it before launching anything
   int sms = 0, per_sm = 0;
   const size_t smem_aff =
-      ((size_t)p6_smem_words_per_slot(P6_AFFINE) * nl8 + p6_smem_words_fixed(P6_AFFINE)) *
-      sizeof(float);
+      ((size_t)p6_smem_words_per_slot(P6_AFFINE) * nl8 + 2 * P6_CRING) * sizeof(float);
   TG_TRY(launch_shape((const void*)hex_le_f32x2_kernel<TG_MODE_HVP, P6_AFFINE>, smem_aff, sms,
                       per_sm));
   if (per_sm <= 0) return TG_ERR_UNSUPPORTED;

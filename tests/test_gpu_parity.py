@@ -392,3 +392,67 @@ def test_nodes_without_elements(cuda):
     fixed[-3:] = 1
     h = en.hvp(None, _t(v, cuda), fixed=fixed)
     assert torch.equal(h[-3:], _t(v, cuda)[-3:]) and torch.count_nonzero(h[-6:-3]) == 0
+
+
+def test_empty_mesh(cuda):
+    """Empty input: the reference rejects a mesh without elements
+    (operator.py:154-155, "Mesh must contain at least one element."), and so does the
+    Operator here; the C ABI itself accepts an empty element list (nothing to do)."""
+    c = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]])
+    e = np.zeros((0, 8), np.int32)
+    with pytest.raises(ValueError, match="at least one element"):
+        Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    from tatva_gb300 import _lib
+    from tatva_gb300._device import ptr, stream
+
+    u = torch.ones(6, dtype=torch.float64, device=cuda)
+    out = torch.full((0, 8, 3), 7.0, dtype=torch.float64, device=cuda)
+    assert _lib.lib().tg_eval(_lib.TG_HEX8, _lib.TG_F64, ptr(u), 2, 3, None, 0, ptr(out),
+                              stream()) == _lib.TG_OK
+
+
+
+def test_periodic_reduced_residual_and_hessian(cuda):
+    """x-periodic Poisson on the unit square with the bottom row fixed: the reduced
+    residual reduce_adjoint(r(lift(u_r))) and the reduced Hessian P^T K P (on the
+    adapt_sparsity pattern) match the oracle."""
+    import scipy.sparse as sps
+
+    from oracle import lifter as olf
+    from tatva_gb300.lifter import Fixed, Lifter, Periodic
+
+    n = 8
+    c, e = om.unit_square(n, n)
+    left = np.where(np.isclose(c[:, 0], 0.0))[0]
+    right = np.where(np.isclose(c[:, 0], 1.0))[0]
+    left, right = left[np.argsort(c[left, 1])], right[np.argsort(c[right, 1])]
+    bottom = np.setdiff1d(np.where(np.isclose(c[:, 1], 0.0))[0], right)
+    N = c.shape[0]
+    lf = Lifter(N, Periodic(right, left), Fixed(bottom, 0.25))
+    ol = olf.Lifter(N, olf.Periodic(right, left), olf.Fixed(bottom, 0.25))
+    op = Operator(Mesh(c, e, device=cuda), element.Tri3())
+    oo = oop.OracleOperator(c, e, oe.Tri3())
+    en, law = materials.Poisson(op, 1.3, 1.0), omat.Poisson(1.3, 1.0)
+    rng = np.random.default_rng(4)
+    ur = rng.standard_normal(lf.size_reduced)
+    u0 = np.zeros(N)
+    r = lf.reduce_adjoint(en.residual(lf.lift(_t(ur, cuda), _t(u0, cuda))))
+    ro = ol.reduce_adjoint(omat.residual(oo, law, ol.lift(ur, u0)))
+    assert rel(r, ro) < F64_TOL
+    # reduced Hessian: P^T K P with the lifting matrix P (slaves copy their masters)
+    cm = sparse.ColoredMatrix.from_csr(sparse.pattern_from_mesh(op.mesh, 1), device=cuda)
+    K = sparse.jacfwd(en.residual, cm)(_t(u0, cuda)).to_csr()
+    free = ol.free_dofs
+    P = sps.lil_matrix((N, free.size))
+    P[free, np.arange(free.size)] = 1.0
+    col_of = {d: i for i, d in enumerate(free)}
+    for s_, m_ in zip(right, left):
+        if m_ in col_of:
+            P[s_, col_of[m_]] = 1.0
+    Kr = (P.T @ K @ P).tocsr()
+    pat = lf.adapt_sparsity(sparse.pattern_from_mesh(op.mesh, 1))
+    assert set(zip(*Kr.nonzero())) <= set(zip(*pat.nonzero()))
+    Ke = omat.element_tangents(oo, law, u0)
+    Ko = omat.assemble_dense(oo, Ke, 1)
+    Kro = P.T.toarray() @ Ko @ P.toarray()
+    assert np.abs(Kr.toarray() - Kro).max() / np.abs(Kro).max() < F64_TOL

@@ -11,7 +11,7 @@ plus fused energies (``materials``), device solvers (``solvers``), the batched
 multi-mesh solver (``batched``) and the request loop (``serving``).
 """
 
-from . import batched, element, lifter, materials, sparse, solvers  # noqa: F401
+from . import batched, compound, element, lifter, materials, sparse, solvers  # noqa: F401
 from ._build import build  # noqa: F401
 from ._lib import BreakdownError, NotConvergedError  # noqa: F401
 from .mesh import Mesh  # noqa: F401
@@ -19,4 +19,4 @@ from .operator import Operator  # noqa: F401
 
 __version__ = "0.1.0"
 __all__ = ["Mesh", "Operator", "element", "sparse", "materials", "lifter", "solvers", "batched",
-           "build"]
+           "compound", "build"]

@@ -194,5 +194,12 @@ def linearized_jacfwd(fn: Callable, colored_matrix: ColoredMatrix, *,
     return _wrapped_linearized
 
 
+def pattern_from_compound(compound_cls, block_wise: bool = False):
+    """Sparsity of a ``Compound`` state on its mesh (tatva/sparse/_extraction.py:117-245)."""
+    from .compound import pattern_from_compound as _pfc
+
+    return _pfc(compound_cls, block_wise=block_wise)
+
+
 __all__ = ["ColoredMatrix", "compute_rows_cols", "decompress", "distance2_colors", "jacfwd",
-           "linearized_jacfwd", "pattern_from_mesh"]
+           "linearized_jacfwd", "pattern_from_compound", "pattern_from_mesh"]

@@ -18,7 +18,7 @@ _TABLE: dict = {}
 
 DEFAULT_CANDIDATES = {
     _lib.TG_TRI3: [(1024, 4096, 128), (2048, 4096, 256), (4096, 4096, 256)],
-    _lib.TG_TET4: [(1024, 4096, 128), (2048, 4096, 256), (4096, 4096, 256)],
+    _lib.TG_TET4: [(1024, 4096, 64), (2048, 4096, 128), (2048, 4096, 256), (4096, 8192, 256)],
     _lib.TG_HEX8: [(512, 4096, 128), (512, 4096, 256), (1024, 4096, 128), (1024, 4096, 256),
                    (2048, 4096, 256), (4096, 8192, 256)],
 }

@@ -18,6 +18,8 @@
 // its own data and the block size -- not on which CTA took it, nor on what else ran.
 // Every loop is bounded by max_outer / max_inner; no CTA waits on another.
 #include <cmath>
+#include <map>
+#include <mutex>
 
 #include "tg_common.cuh"
 #include "tg_dispatch.cuh"
@@ -414,8 +416,18 @@ extern "C" int tg_batch_solve(const tg_batch_desc* desc, int64_t n_rows, const d
   TG_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
   TG_TRY(cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"));
   auto go = [&](auto kern, int nt) -> int {
-    TG_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "tg_batch_solve: shared memory attribute"));
+    {
+      // the attribute only grows: graphs captured with larger systems stay launchable
+      static std::mutex mu;
+      static std::map<std::pair<const void*, int>, size_t> attr;
+      std::lock_guard<std::mutex> g(mu);
+      size_t& cur = attr[std::make_pair((const void*)kern, dev)];
+      if (smem > cur) {
+        TG_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                          "tg_batch_solve: shared memory attribute"));
+        cur = smem;
+      }
+    }
     int per_sm = 0;
     TG_TRY(cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem),
                       "tg_batch_solve: occupancy"));

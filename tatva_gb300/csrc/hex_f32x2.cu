@@ -527,9 +527,13 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
 
 // Per (kernel, device, shared-memory size): SM count and resident CTAs per SM, set up
 // once (the attribute call and the occupancy query cost more than a launch).
+// The dynamic shared-memory attribute of a kernel only ever grows (to the largest size
+// requested so far): lowering it would break launches of larger plans that reuse a
+// cached shape, and CUDA graphs captured with them.
 static int launch_shape(const void* k, size_t smem, int& sms, int& per_sm) {
   static std::mutex mu;
   static std::map<std::tuple<const void*, int, size_t>, std::pair<int, int>> cache;
+  static std::map<std::pair<const void*, int>, size_t> attr;
   int dev = 0;
   TG_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
   std::lock_guard<std::mutex> g(mu);
@@ -541,8 +545,12 @@ static int launch_shape(const void* k, size_t smem, int& sms, int& per_sm) {
     TG_TRY(cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
                       "shared memory limit"));
     if (smem <= (size_t)optin) {
-      TG_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                        "hex f32x2: shared memory attribute"));
+      size_t& cur = attr[std::make_pair(k, dev)];
+      if (smem > cur) {
+        TG_TRY(cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                          "hex f32x2: shared memory attribute"));
+        cur = smem;
+      }
       TG_TRY(cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, P6_THREADS, smem),
                         "hex f32x2: occupancy"));
     }

@@ -135,18 +135,26 @@ class Operator:
              threads: int | None = None):
         """Element-block plan of the fused kernels (cached per tuning)."""
         from . import autotune
-        from .plan import BlockPlan, DEFAULT_MAX_LOCAL
+        from .plan import BlockPlan, DEFAULT_MAX_LOCAL, DEFAULT_THREADS
 
         if block_elems is None and max_local_nodes is None and threads is None:
             cfg = autotune.lookup(self)
+            if cfg == (None, None, None) and self.element.tg_id == _lib.TG_HEX8:
+                # Hex8: 512-element blocks suit the parallelepiped kernels; meshes whose
+                # blocks are mostly general (per-QP path) run faster with 1024 / 128
+                p512 = self.plan(512, DEFAULT_MAX_LOCAL, DEFAULT_THREADS[_lib.TG_HEX8])
+                if 2 * p512.sizes["n_affine_blocks"] >= p512.sizes["n_blocks"]:
+                    return p512
+                return self.plan(1024, DEFAULT_MAX_LOCAL, 128)
             block_elems, max_local_nodes, threads = cfg
-        key = ("plan", block_elems, max_local_nodes or DEFAULT_MAX_LOCAL, threads or 256)
+        threads = threads or DEFAULT_THREADS[self.element.tg_id]
+        key = ("plan", block_elems, max_local_nodes or DEFAULT_MAX_LOCAL, threads)
         if key not in self._cache:
             self._cache[key] = BlockPlan(self.element.tg_id, self.mesh.elements_host(),
                                          self.mesh.coords_host(), self.device,
                                          block_elems=block_elems,
                                          max_local_nodes=max_local_nodes or DEFAULT_MAX_LOCAL,
-                                         threads=threads or 256)
+                                         threads=threads)
         return self._cache[key]
 
     def unused_nodes(self) -> torch.Tensor:

@@ -72,3 +72,36 @@ def stretched_kuhn(n: int, device, jitter: float = 0.2, seed: int = 0, mu: float
 
 
 __all__ = ["clamped_brick", "stretched_kuhn"]
+
+
+def _main(argv=None) -> None:
+    """``python -m tatva_gb300.problems {brick,kuhn,kuhn-le} N [repeats] [f32|f64]``: run
+    the fused HVP of a benchmark problem ``repeats`` times (a workload driver for
+    profiling)."""
+    import sys
+
+    from . import _lib
+    from .materials import LinearElastic
+
+    args = list(sys.argv[1:] if argv is None else argv)
+    name = args[0] if args else "brick"
+    n = int(args[1]) if len(args) > 1 else 64
+    reps = int(args[2]) if len(args) > 2 else 3
+    dtype = torch.float64 if (len(args) > 3 and args[3] == "f64") else torch.float32
+    if name == "brick":
+        P = clamped_brick(n, "cuda")
+        en, u = P["energy"], None
+    else:
+        P = stretched_kuhn(n, "cuda")
+        en = P["energy"] if name == "kuhn" else LinearElastic(P["op"], 1.0, 1.0)
+        u = None if name != "kuhn" else torch.zeros(en.n_dofs, dtype=dtype, device="cuda")
+    v = torch.ones(en.n_dofs, dtype=dtype, device="cuda")
+    y = torch.empty_like(v)
+    for _ in range(reps):
+        en.apply(_lib.TG_MODE_HVP, u, v, out=y)
+    torch.cuda.synchronize()
+    print(name, n, en.n_dofs, float(y.abs().sum()))
+
+
+if __name__ == "__main__":
+    _main()

@@ -221,8 +221,11 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ndof / value / 1e6,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"hex8 linear-elastic HVP, brick {n}^3 sample of the 128^3 brick "
-                               "(E=1, nu=0.3)", "l2": "host CPU"},
+        "config": {"workload": f"hex8 linear-elastic HVP, structured brick {N_CELLS}^3 "
+                               f"({N_CELLS ** 3} elements, {3 * (N_CELLS + 1) ** 3} dofs), E=1 "
+                               "nu=0.3, 2x2x2 Gauss",
+                   "l2": "host CPU", "parallelism": "host cores",
+                   "step": f"one HVP over a {n}^3 sample brick of the workload"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"numpy restatement of the HVP on a {n}^3 brick "
                                    f"({ndof} dofs), elements split over {cores} processes"},

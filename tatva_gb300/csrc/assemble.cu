@@ -398,6 +398,100 @@ struct HasAffinePath {
                                 MODE != TG_MODE_DIAG;
 };
 
+// Linear elasticity on an axis-aligned box: R = diag(r) (r_k = 1 / Jm_kk), so every
+// product with R is one multiply and the Gram matrix is diag(r_k^2).  Same monomial
+// algebra as hex_modal_apply, with the zeros of R removed (about a third of the
+// arithmetic, which bounds the FP64 kernel on this GPU).
+template <class T, int P, int Q>
+__device__ __forceinline__ void le_two_dir_box(const T (&r)[3], const T (&rr)[3], const T (&gp)[3],
+                                               const T (&gq)[3], T mu, T lam, T (&Fp)[3],
+                                               T (&Fq)[3]) {
+  const T a_pp = gp[P] * r[P], a_pq = gp[Q] * r[Q];
+  const T a_qp = gq[P] * r[P], a_qq = gq[Q] * r[Q];
+  const T lt = lam * (a_pp + a_qq);
+  const T c1 = mu * rr[P], d2 = mu * rr[Q];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    Fp[j] = c1 * gp[j];
+    Fq[j] = d2 * gq[j];
+  }
+  Fp[P] += (mu * a_pp + lt) * r[P];
+  Fp[Q] += (mu * a_qp) * r[Q];
+  Fq[P] += (mu * a_pq) * r[P];
+  Fq[Q] += (mu * a_qq + lt) * r[Q];
+}
+
+template <class T>
+__device__ __forceinline__ void hex_le_modal_box(const T (&r)[3], T detJm, T mu, T lam,
+                                                 const T (&W)[8][3], T (&Y)[8][3]) {
+  const T g2 = T(HEX_GAUSS) * T(HEX_GAUSS);
+  const T s0 = detJm * T(1.0 / 64);
+  const T s1 = s0 * g2;
+  const T s2 = s1 * g2;
+  T M[3][8];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+#pragma unroll
+    for (int a = 0; a < 8; ++a) M[j][hex_t(a)] = W[a][j];
+    hadamard8(M[j]);
+  }
+  T dM[3][8];
+  {  // constant monomial: directions (x, y, z) carry (M1, M2, M4)
+    T H[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) H[j][k] = r[k] * M[j][1 << k];
+    const T m0 = mu * s0;
+    const T lt = (lam * s0) * (H[0][0] + H[1][1] + H[2][2]);
+    T Pm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      Pm[i][i] = m0 * (H[i][i] + H[i][i]) + lt;
+#pragma unroll
+      for (int j = i + 1; j < 3; ++j) {
+        Pm[i][j] = m0 * (H[i][j] + H[j][i]);
+        Pm[j][i] = Pm[i][j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      dM[j][0] = T(0);
+      dM[j][1] = Pm[j][0] * r[0];
+      dM[j][2] = Pm[j][1] * r[1];
+      dM[j][4] = Pm[j][2] * r[2];
+    }
+  }
+  const T rr[3] = {r[0] * r[0], r[1] * r[1], r[2] * r[2]};
+  const T mu1 = mu * s1, lam1 = lam * s1;
+  T g12[3], g13[3], g23[3], Fp[3], Fq[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    g12[j] = M[j][3];
+    g13[j] = M[j][5];
+    g23[j] = M[j][6];
+  }
+  le_two_dir_box<T, 1, 2>(r, rr, g12, g13, mu1, lam1, Fp, Fq);  // monomial x
+#pragma unroll
+  for (int j = 0; j < 3; ++j) { dM[j][3] = Fp[j]; dM[j][5] = Fq[j]; }
+  le_two_dir_box<T, 0, 2>(r, rr, g12, g23, mu1, lam1, Fp, Fq);  // monomial y
+#pragma unroll
+  for (int j = 0; j < 3; ++j) { dM[j][3] += Fp[j]; dM[j][6] = Fq[j]; }
+  le_two_dir_box<T, 0, 1>(r, rr, g13, g23, mu1, lam1, Fp, Fq);  // monomial z
+#pragma unroll
+  for (int j = 0; j < 3; ++j) { dM[j][5] += Fp[j]; dM[j][6] += Fq[j]; }
+  // yz, xz, xy: (mu tr(Gm) + (mu + lam) r_j^2) M123_j
+  const T a = (mu * s2) * (rr[0] + rr[1] + rr[2]), ml2 = (mu + lam) * s2;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) dM[j][7] = (ml2 * rr[j] + a) * M[j][7];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    hadamard8_t(dM[j]);
+#pragma unroll
+    for (int a8 = 0; a8 < 8; ++a8) Y[a8][j] = dM[j][hex_t(a8)];
+  }
+}
+
 template <int ET, int MAT, class T, int MODE, bool AFFINE>
 __device__ __forceinline__ void element_apply(
     T p0, T p1, const T (&X)[Elem<ET>::NN][Elem<ET>::D],
@@ -663,6 +757,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   const int ne = p.blk_elem_ptr[b + 1] - e_base;
   const int c_begin = p.blk_color_ptr[b];
   const int c_last = p.blk_color_ptr[b + 1] - 1;
+  const bool box = b < p.n_diag_blocks;
   for (int k0 = 0; k0 < ne; k0 += nt) {
     const int k = k0 + threadIdx.x;
     const bool act = k < ne;
@@ -675,7 +770,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
 #pragma unroll
       for (int a = 0; a < 8; ++a) q[a] = lc[a];
       // geometry: Jm = 8 J, rows 4 (x_1 - x_0), 4 (x_3 - x_0), 4 (x_4 - x_0)
-      T Jm[3][3], R[3][3], pad;
+      T Jm[3][3], pad;
       {
         T x0[3], xe[3];
         ld4<T>(XS + q[0] * 4, x0[0], x0[1], x0[2], pad);
@@ -687,7 +782,6 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
           for (int d = 0; d < 3; ++d) Jm[i][d] = T(4) * (xe[d] - x0[d]);
         }
       }
-      const T detJm = inv3(Jm, R);
       T W[8][V];
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
@@ -698,8 +792,22 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
         }
       }
       const T k0p = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
-      hex_modal_apply<MAT, T>(R, detJm, k0p, lam, W, Y);
+      bool done_box = false;
+      if constexpr (MAT == TG_LINEAR_ELASTIC) {
+        if (box) {  // axis-aligned box (host-verified for the whole block)
+          const T r[3] = {T(1) / Jm[0][0], T(1) / Jm[1][1], T(1) / Jm[2][2]};
+          hex_le_modal_box<T>(r, Jm[0][0] * Jm[1][1] * Jm[2][2], k0p, lam, W, Y);
+          done_box = true;
+        }
+      }
+      if (!done_box) {
+        T R[3][3];
+        const T detJm = inv3(Jm, R);
+        hex_modal_apply<MAT, T>(R, detJm, k0p, lam, W, Y);
+      }
       if constexpr (MODE == TG_MODE_RESIDUAL && MAT == TG_POISSON) {
+        T Rn[3][3];
+        const T detJm = inv3(Jm, Rn);
         const T fd = p1 * detJm * T(1.0 / 512);
 #pragma unroll
         for (int a = 0; a < 8; ++a) Y[a][0] -= fd;

@@ -50,6 +50,16 @@ __device__ __forceinline__ void cp_async_wait0() {
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
+// L2 prefetch of the 128-byte lines that hold [p, p + bytes), spread over the CTA's
+// threads.  Every line issued contains at least one byte of the range.
+__device__ __forceinline__ void prefetch_l2_range(const void* p, size_t bytes, int tid, int nt) {
+  if (bytes == 0) return;
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(127);
+  const uintptr_t a1 = reinterpret_cast<uintptr_t>(p) + bytes;
+  for (uintptr_t a = a0 + (uintptr_t)tid * 128; a < a1; a += (uintptr_t)nt * 128)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
+
 __device__ __forceinline__ void had8(f2 (&m)[8]) {
 #pragma unroll
   for (int h = 1; h < 8; h <<= 1)
@@ -329,6 +339,20 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
       }
     }
   };
+  // the per-element and per-node plan arrays of block b that the compute reads with
+  // plain loads (edge terms, local connectivity, partial slots): into L2 one block
+  // ahead, so that those loads do not wait on DRAM
+  auto prefetch_block = [&](int b) {
+    const int e0 = __ldg(p.blk_elem_ptr + b), ne = __ldg(p.blk_elem_ptr + b + 1) - e0;
+    const int n0 = __ldg(p.blk_node_ptr + b), nl = __ldg(p.blk_node_ptr + b + 1) - n0;
+    if (GEO) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        prefetch_l2_range(p.box_geom32 + (int64_t)c * p.n_elems + e0, (size_t)ne * 4, tid, NT);
+    }
+    prefetch_l2_range(reinterpret_cast<const uint4*>(p.lconn) + e0, (size_t)ne * 16, tid, NT);
+    prefetch_l2_range(p.lnode_slot + n0, (size_t)nl * 4, tid, NT);
+  };
   auto load_lconn4 = [&](int b, uint4 (&LC)[P6_EPT]) {
     const int e0 = __ldg(p.blk_elem_ptr + b), ne = __ldg(p.blk_elem_ptr + b + 1) - e0;
 #pragma unroll
@@ -344,6 +368,7 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
   if (bi < nblk) issue_ids(b_begin + bi, 0);
   if (bi < nblk) issue_cofs(b_begin + bi, 0);
   cp_async_commit();
+  if (bi < nblk) prefetch_block(b_begin + bi);
   cp_async_wait0();
   __syncthreads();
   if (bi < nblk) issue_data(b_begin + bi, 0, 0);
@@ -372,6 +397,7 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
     if (bi + stride < nblk) issue_data(b + stride, s ^ 1, s ^ 1);
     if (bi + 2 * stride < nblk) issue_ids(b + 2 * stride, s);
     cp_async_commit();
+    if (bi + stride < nblk) prefetch_block(b + stride);
 
     const float* X = sm + s * BW * nl8;
     float* W = const_cast<float*>(X) + (BW - 4) * nl8;

@@ -157,11 +157,18 @@ typedef struct tg_block_plan {
   const int32_t* lnode_smem;     /* [sum L_b] shared-memory slot of the local node */
   const int32_t* shared_node;    /* [n_shared] global node id                      */
   const int32_t* shared_ptr;     /* [n_shared+1]                                   */
-  const int32_t* shared_slots;   /* [n_partials] slots in summation order          */
+  const int32_t* shared_slots;   /* [n_partials] slots in summation order; NULL:
+                                  * identity (the k-th partial sits in slot k)    */
   /* optional, FP32 linear elasticity on Hex8 boxes: [3][n_elems] edge terms
    * 4(x1-x0), 4(y3-y0), 4(z4-z0) of the element positions of the box blocks, filled
    * by tg_plan_box_geometry; NULL: the kernel computes them from coordinates.     */
   const float* box_geom32;
+  int32_t n_lattice_blocks;      /* Hex8: blocks [0, n_lattice_blocks) (a prefix of
+                                    the box blocks) hold 8 x 8 x 8 boxes on 9 x 9 x 9
+                                    local nodes numbered l = i + 9 j + 81 k, element
+                                    corner a at (i,j,k) + (0,0,0) (1,0,0) (1,1,0)
+                                    (0,1,0) (0,0,1) (1,0,1) (1,1,1) (0,1,1); 0: none */
+  int32_t reserved0;
 } tg_block_plan;
 
 /* Material parameters.  kind = TG_POISSON: p0 = kappa, p1 = f (source);
@@ -181,9 +188,9 @@ typedef struct tg_material {
 TG_API int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int64_t n_nodes,
                   const double* coords, int dim, int block_elems, int max_local_nodes,
                   void** handle);
-/* sizes[0..11] = n_blocks, n_elems, color_ofs_len, total_local_nodes, n_shared,
+/* sizes[0..12] = n_blocks, n_elems, color_ofs_len, total_local_nodes, n_shared,
  * n_partials, max_local_nodes, max_block_colors, stride, n_affine_blocks,
- * n_diag_blocks, max_block_elems.  Local node l of a block lives in shared-memory
+ * n_diag_blocks, max_block_elems, n_lattice_blocks.  Local node l of a block lives in shared-memory
  * slot lnode_smem[l] < 8 ceil(L_b / 8), chosen so that the nodes one quarter-warp
  * reads at an element corner fall in distinct bank quads; lconn stores slots.   */
 TG_API int tg_plan_sizes(const void* handle, int64_t* sizes);

@@ -64,6 +64,8 @@ class BlockPlan(ctypes.Structure):
         ("shared_ptr", c_void_p),
         ("shared_slots", c_void_p),
         ("box_geom32", c_void_p),
+        ("n_lattice_blocks", c_int32),
+        ("reserved0", c_int32),
     ]
 
 

@@ -629,7 +629,7 @@ __global__ void shared_reduce_kernel(const tg_block_plan p, const T* __restrict_
   for (int i = 0; i < V; ++i) acc[i] = T(0);
   const int k1 = p.shared_ptr[s + 1];
   for (int k = p.shared_ptr[s]; k < k1; ++k) {
-    const int64_t slot = p.shared_slots[k];
+    const int64_t slot = p.shared_slots ? p.shared_slots[k] : k;
 #pragma unroll
     for (int i = 0; i < V; ++i) acc[i] += partials[slot * V + i];
   }

@@ -551,6 +551,273 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
   cp_async_wait0();
 }
 
+// ------------------------------------------------------------------ lattice blocks
+// Box blocks whose 512 elements form an 8 x 8 x 8 lattice over 9 x 9 x 9 local nodes
+// numbered l = i + 9 j + 81 k (blocks [0, plan.n_lattice_blocks)).  Warp w = jh + 2 kh
+// owns the element columns (i, j = 4 jh + jl), lane = i + 8 jl, and sweeps the element
+// layers 4 kh .. 4 kh + 3 two at a time, one per f32x2 lane, with the box law of the
+// kernel above (same inputs, same bits per element).  A node's sum over one warp's
+// elements is formed in registers (the layer carried up the sweep) and by lane shuffles
+// (along i, then along j) in a fixed order; the 153 nodes that two or four warps touch
+// (row j = 4 and layer k = 4) go through shared memory and are added in warp order
+// after the sweep.  No element colouring, no barrier inside the sweep, no element
+// connectivity: a block reads its 729 node ids and partial slots, the input vector at
+// those nodes and the 27 coordinates of its grid lines.
+constexpr int LT_THREADS = 128;
+constexpr int LT_NODES = 729, LT_RING = 732, LT_MERGE = 153;
+// W [2][729] float4 | merge parts [4][153] float4 | ids [2][732] | slots [2][732] |
+// grid lines [2][32]
+constexpr size_t LT_SMEM = (2 * LT_NODES + 4 * LT_MERGE) * 16 + 4 * LT_RING * 4 + 2 * 32 * 4;
+
+__device__ __forceinline__ void cp_async_wait1() {
+  asm volatile("cp.async.wait_group 1;" ::: "memory");
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(LT_THREADS, 4)
+    hex_le_lattice_kernel(const tg_block_plan p, const float* __restrict__ coords,
+                          const float* __restrict__ fin, const uint8_t* __restrict__ fixed,
+                          const float* __restrict__ vin, float* __restrict__ y,
+                          float* __restrict__ partials, float mu_s, float lam_s) {
+  extern __shared__ __align__(16) float sm[];
+  float4* const W = reinterpret_cast<float4*>(sm);
+  float4* const Pm = W + 2 * LT_NODES;
+  int* const ids = reinterpret_cast<int*>(Pm + 4 * LT_MERGE);
+  int* const slots = ids + 2 * LT_RING;
+  float* const geo = reinterpret_cast<float*>(slots + 2 * LT_RING);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nblk = p.n_lattice_blocks, stride = gridDim.x;
+  const int64_t nbase = __ldg(p.blk_node_ptr);
+
+  // node ids and partial slots of block b into ring entry r
+  auto issue_meta = [&](int b, int r) {
+    const int64_t n0 = nbase + (int64_t)LT_NODES * b;
+    for (int l = tid; l < LT_NODES; l += LT_THREADS) {
+      cp_async4(ids + r * LT_RING + l, p.lnode_gid + n0 + l);
+      cp_async4(slots + r * LT_RING + l, p.lnode_slot + n0 + l);
+    }
+  };
+  // input values of the block whose ids are in ring entry r into buffer r (8 nodes x 3
+  // components per warp instruction), and its grid lines: x of nodes (i, 0, 0), y of
+  // (0, j, 0), z of (0, 0, k)
+  auto issue_data = [&](int r) {
+    float* Wr = reinterpret_cast<float*>(W + r * LT_NODES);
+    const int* id = ids + r * LT_RING;
+    const int sub = lane / 3, d = lane - 3 * sub;
+    if (lane < 24)
+      for (int l = warp * 8 + sub; l < LT_NODES; l += 32)
+        cp_async4(Wr + l * 4 + d, fin + (int64_t)id[l] * 3 + d);
+    if (tid < 27) {
+      const int a = tid / 9, q = tid - 9 * a;
+      const int l = a == 0 ? q : (a == 1 ? 9 * q : 81 * q);
+      cp_async4(geo + r * 32 + tid, coords + (int64_t)id[l] * 3 + a);
+    }
+  };
+
+  int bi = blockIdx.x;
+  if (bi < nblk) issue_meta(bi, 0);
+  cp_async_commit();
+  cp_async_wait0();
+  __syncthreads();
+  if (bi < nblk) issue_data(0);
+  cp_async_commit();
+  if (bi + stride < nblk) issue_meta(bi + stride, 1);
+  cp_async_commit();
+
+  const int jh = warp & 1, kh = warp >> 1;
+  const int i = lane & 7, jl = lane >> 3, j = 4 * jh + jl, k0 = 4 * kh;
+  const f2 mu = f2_bcast(mu_s), lam = f2_bcast(lam_s);
+  for (int it = 0; bi < nblk; ++it, bi += stride) {
+    const int s = it & 1;
+    cp_async_wait1();  // this block's data (the newest group, the next block's ids, may pend)
+    __syncthreads();
+    const float4* Ws = W + s * LT_NODES;
+    const int* id = ids + s * LT_RING;
+    const int* sl = slots + s * LT_RING;
+    if (MODE == TG_MODE_HVP && fixed) {
+      float* Wf = reinterpret_cast<float*>(W + s * LT_NODES);
+      for (int l = tid; l < LT_NODES; l += LT_THREADS) {
+        const int64_t g = id[l];
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          if (fixed[g * 3 + d]) Wf[l * 4 + d] = 0.f;
+      }
+      __syncthreads();
+    }
+
+    // final block-local sum of node l: the node's own value if no other block touches it,
+    // else its partial slot
+    auto emit = [&](int l, float v0, float v1, float v2) {
+      const int64_t g = id[l];
+      const int q = sl[l];
+      const float v[3] = {v0, v1, v2};
+      if (q < 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const int64_t dof = g * 3 + d;
+          float val = v[d];
+          if (fixed && fixed[dof]) val = (MODE == TG_MODE_HVP) ? vin[dof] : 0.f;
+          y[dof] = val;
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) partials[(int64_t)q * 3 + d] = v[d];
+      }
+    };
+    // this warp's sum at node (ni, nj, L): emitted, or parked for the merge when another
+    // warp also touches the node
+    auto put = [&](int ni, int nj, int L, const float (&v)[3]) {
+      if (nj == 4 || L == 4) {
+        const int m = (nj == 4) ? ni + 9 * L : 81 + ni + 9 * (nj < 4 ? nj : nj - 1);
+        Pm[warp * LT_MERGE + m] = make_float4(v[0], v[1], v[2], 0.f);
+      } else {
+        emit(ni + 9 * nj + 81 * L, v[0], v[1], v[2]);
+      }
+    };
+    // Q[t][c]: this lane's column values at the corners t = di + 2 dj of layer L
+    auto reduce_put = [&](float (&Q)[4][3], int L) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float a = __shfl_up_sync(0xffffffffu, Q[1][c], 1);
+        const float b = __shfl_up_sync(0xffffffffu, Q[3][c], 1);
+        if (i > 0) {
+          Q[0][c] += a;
+          Q[2][c] += b;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float a = __shfl_up_sync(0xffffffffu, Q[2][c], 8);
+        const float b = __shfl_up_sync(0xffffffffu, Q[3][c], 8);
+        if (jl > 0) {
+          Q[0][c] += a;
+          Q[1][c] += b;
+        }
+      }
+      put(i, j, L, Q[0]);
+      if (i == 7) put(8, j, L, Q[1]);
+      if (jl == 3) put(i, j + 1, L, Q[2]);
+      if (i == 7 && jl == 3) put(8, j + 1, L, Q[3]);
+    };
+    auto load_layer = [&](int L, float (&o)[4][3]) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const float4 w = Ws[(i + (t & 1)) + 9 * (j + (t >> 1)) + 81 * L];
+        o[t][0] = w.x;
+        o[t][1] = w.y;
+        o[t][2] = w.z;
+      }
+    };
+
+    const float* G = geo + s * 32;
+    const float hx = 4.f * (G[i + 1] - G[i]);
+    const float hy = 4.f * (G[9 + j + 1] - G[9 + j]);
+    const float rx = __frcp_rn(hx), ry = __frcp_rn(hy);
+    const float hxy = hx * hy;
+    float cur[4][3], C[4][3];
+    load_layer(k0, cur);
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) C[t][c] = 0.f;
+#pragma unroll 1
+    for (int ps = 0; ps < 2; ++ps) {
+      const int k = k0 + 2 * ps;
+      float mid[4][3], top[4][3];
+      load_layer(k + 1, mid);
+      load_layer(k + 2, top);
+      f2 M[3][8];
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          M[c][t] = f2_make(cur[t][c], mid[t][c]);
+          M[c][t + 4] = f2_make(mid[t][c], top[t][c]);
+        }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) had8(M[c]);
+      const float hzA = 4.f * (G[18 + k + 1] - G[18 + k]);
+      const float hzB = 4.f * (G[18 + k + 2] - G[18 + k + 1]);
+      f2 R[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) R[a][b] = f2_zero();
+      R[0][0] = f2_bcast(rx);
+      R[1][1] = f2_bcast(ry);
+      R[2][2] = f2_make(__frcp_rn(hzA), __frcp_rn(hzB));
+      const f2 detJm = f2_make(hxy * hzA, hxy * hzB);
+      f2 dM[3][8];
+      le_modal_pair<true>(R, detJm, mu, lam, M, dM);
+      float YA[8][3], YB[8][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        had8t(dM[c]);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) f2_split(dM[c][t], YA[t][c], YB[t][c]);
+      }
+      float Q[4][3];
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Q[t][c] = C[t][c] + YA[t][c];
+      reduce_put(Q, k);
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Q[t][c] = YA[t + 4][c] + YB[t][c];
+      reduce_put(Q, k + 1);
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          C[t][c] = YB[t + 4][c];
+          cur[t][c] = top[t][c];
+        }
+      if (ps == 0) {  // the next block's ids have landed: start its data
+        cp_async_wait0();
+        __syncthreads();
+        if (bi + stride < nblk) issue_data(s ^ 1);
+        cp_async_commit();
+      }
+    }
+    reduce_put(C, k0 + 4);
+    __syncthreads();  // every warp's merge parts are in place
+
+    for (int m = tid; m < LT_MERGE; m += LT_THREADS) {
+      int ni, nj, L;
+      float4 a;
+      if (m < 81) {
+        ni = m % 9;
+        L = m / 9;
+        nj = 4;
+      } else {
+        const int r = m - 81, jj = r / 9;
+        ni = r - 9 * jj;
+        nj = jj < 4 ? jj : jj + 1;
+        L = 4;
+      }
+      if (nj == 4 && L == 4) {
+        const float4 a0 = Pm[m], a1 = Pm[LT_MERGE + m], a2 = Pm[2 * LT_MERGE + m],
+                     a3 = Pm[3 * LT_MERGE + m];
+        a = make_float4(((a0.x + a1.x) + a2.x) + a3.x, ((a0.y + a1.y) + a2.y) + a3.y,
+                        ((a0.z + a1.z) + a2.z) + a3.z, 0.f);
+      } else {
+        // row j = 4: warps (jh 0, jh 1) of the layer's half; layer 4: warps (kh 0, kh 1)
+        const int w0 = (nj == 4) ? 2 * (L < 4 ? 0 : 1) : (nj < 4 ? 0 : 1);
+        const int w1 = (nj == 4) ? w0 + 1 : w0 + 2;
+        const float4 a0 = Pm[w0 * LT_MERGE + m], a1 = Pm[w1 * LT_MERGE + m];
+        a = make_float4(a0.x + a1.x, a0.y + a1.y, a0.z + a1.z, 0.f);
+      }
+      emit(ni + 9 * nj + 81 * L, a.x, a.y, a.z);
+    }
+    __syncthreads();  // ring entry s and the merge parts are free
+    if (bi + 2 * stride < nblk) issue_meta(bi + 2 * stride, s);
+    cp_async_commit();
+  }
+  cp_async_wait0();
+}
+
 // Per (kernel, device, shared-memory size): SM count and resident CTAs per SM, set up
 // once (the attribute call and the occupancy query cost more than a launch).
 // The dynamic shared-memory attribute of a kernel only ever grows (to the largest size
@@ -605,16 +872,33 @@ static int launch6(const tg_block_plan* plan, int b0, int b1, const float* coord
 }
 
 template <int MODE>
+static int launch_lattice(const tg_block_plan* plan, const float* coords, const float* fin,
+                          const uint8_t* fixed, const float* vin, float* y, float* partials,
+                          float mu, float lam, cudaStream_t st) {
+  const int n = plan->n_lattice_blocks;
+  if (n <= 0) return TG_OK;
+  auto k = hex_le_lattice_kernel<MODE>;
+  int sms = 0, per_sm = 0;
+  TG_TRY(launch_shape((const void*)k, LT_SMEM, sms, per_sm));
+  if (per_sm <= 0) return TG_ERR_UNSUPPORTED;
+  const int grid = std::max(1, std::min(n, sms * per_sm));
+  k<<<grid, LT_THREADS, LT_SMEM, st>>>(*plan, coords, fin, fixed, vin, y, partials, mu, lam);
+  return launch_check("hex lattice kernel");
+}
+
+template <int MODE>
 static int launch_modes(const tg_block_plan* plan, const float* coords, const float* fin,
                         const uint8_t* fixed, const float* vin, float* y, float* partials,
                         float mu, float lam, int nl8, cudaStream_t st) {
   const int n_aff = plan->n_affine_blocks, n_diag = plan->n_diag_blocks;
+  const int n_lat = plan->n_lattice_blocks;
+  TG_TRY(launch_lattice<MODE>(plan, coords, fin, fixed, vin, y, partials, mu, lam, st));
   if (plan->box_geom32) {
-    TG_TRY((launch6<MODE, P6_BOX_GEOM>(plan, 0, n_diag, coords, fin, fixed, vin, y, partials, mu,
-                                       lam, nl8, st)));
+    TG_TRY((launch6<MODE, P6_BOX_GEOM>(plan, n_lat, n_diag, coords, fin, fixed, vin, y, partials,
+                                       mu, lam, nl8, st)));
   } else {
-    TG_TRY((launch6<MODE, P6_BOX>(plan, 0, n_diag, coords, fin, fixed, vin, y, partials, mu, lam,
-                                  nl8, st)));
+    TG_TRY((launch6<MODE, P6_BOX>(plan, n_lat, n_diag, coords, fin, fixed, vin, y, partials, mu,
+                                  lam, nl8, st)));
   }
   return launch6<MODE, P6_AFFINE>(plan, n_diag, n_aff, coords, fin, fixed, vin, y, partials, mu,
                                   lam, nl8, st);
@@ -628,6 +912,8 @@ int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords
   if (plan->max_local_nodes > P6_MAX_LOCAL || plan->max_block_elems > P6_MAX_ELEMS)
     return TG_ERR_UNSUPPORTED;
   if (n_diag < 0 || n_diag > n_aff) return set_error(TG_ERR_VALUE, "plan.n_diag_blocks out of range");
+  if (plan->n_lattice_blocks < 0 || plan->n_lattice_blocks > n_diag)
+    return set_error(TG_ERR_VALUE, "plan.n_lattice_blocks out of range");
   const int nl8 = (plan->max_local_nodes + 7) & ~7;
   // the general kernel needs the most shared memory: check it before launching anything
   int sms = 0, per_sm = 0;

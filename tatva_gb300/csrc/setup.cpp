@@ -80,7 +80,7 @@ struct Pattern {
 
 struct Plan {
   int32_t n_blocks = 0, n_elems = 0, npad = 4, max_local = 0, max_colors = 0, n_affine = 0,
-          n_diag = 0, max_elems = 0;
+          n_diag = 0, max_elems = 0, n_lattice = 0;
   std::vector<int32_t> blk_elem_ptr, blk_color_ptr, color_ofs, blk_node_ptr, elem_id, lnode_gid,
       lnode_slot, lnode_smem, shared_node, shared_ptr, shared_slots;
   std::vector<uint16_t> lconn;
@@ -138,6 +138,72 @@ bool hex_box_exact(const double* coords, const int32_t* nodes) {
       const T b = (T)coords[(int64_t)nodes[0] * 3 + k];
       if (a - b != T(0)) return false;
     }
+  return true;
+}
+
+// Lattice blocks: 8 x 8 x 8 Hex8 boxes on a 9 x 9 x 9 grid of nodes.
+constexpr int LAT_N = 8, LAT_NN = LAT_N + 1, LAT_NODES = LAT_NN * LAT_NN * LAT_NN;
+
+// Grid positions of a block's nodes: lat[l] = ix + 9 iy + 81 iz for node ids[l] when
+// the nodes' coordinates take exactly 9 distinct values per axis and fill the 9 x 9 x 9
+// grid once; false otherwise.
+bool lattice_positions(const double* coords, const std::vector<int32_t>& ids,
+                       std::vector<int32_t>& lat) {
+  if ((int)ids.size() != LAT_NODES) return false;
+  std::vector<double> ax[3];
+  for (int d = 0; d < 3; ++d) {
+    ax[d].reserve(ids.size());
+    for (int32_t g : ids) ax[d].push_back(coords[(int64_t)g * 3 + d]);
+    std::sort(ax[d].begin(), ax[d].end());
+    ax[d].erase(std::unique(ax[d].begin(), ax[d].end()), ax[d].end());
+    if ((int)ax[d].size() != LAT_NN) return false;
+  }
+  lat.assign(ids.size(), -1);
+  std::vector<char> seen(LAT_NODES, 0);
+  for (size_t l = 0; l < ids.size(); ++l) {
+    int p = 0;
+    for (int d = 2; d >= 0; --d) {
+      const double x = coords[(int64_t)ids[l] * 3 + d];
+      p = p * LAT_NN + (int)(std::lower_bound(ax[d].begin(), ax[d].end(), x) - ax[d].begin());
+    }
+    if (seen[p]) return false;
+    seen[p] = 1;
+    lat[l] = p;
+  }
+  return true;
+}
+
+// Lattice test of a Hex8 box block (elements key[k0, k1)): 512 elements whose node a
+// sits at grid offset (dx, dy, dz)_a = (0,0,0) (1,0,0) (1,1,0) (0,1,0) (0,0,1) (1,0,1)
+// (1,1,1) (0,1,1) from node 0, one element per grid cell.
+bool hex_block_lattice(const double* coords, const int32_t* conn,
+                       const std::vector<std::pair<uint64_t, int32_t>>& key, int32_t k0,
+                       int32_t k1) {
+  if (k1 - k0 != LAT_N * LAT_N * LAT_N) return false;
+  std::vector<int32_t> ids;
+  ids.reserve((size_t)(k1 - k0) * 8);
+  for (int32_t k = k0; k < k1; ++k)
+    for (int a = 0; a < 8; ++a) ids.push_back(conn[(int64_t)key[k].second * 8 + a]);
+  std::sort(ids.begin(), ids.end());
+  ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+  std::vector<int32_t> lat;
+  if (!lattice_positions(coords, ids, lat)) return false;
+  static const int off[8] = {0, 1, 1 + LAT_NN, LAT_NN, LAT_NN * LAT_NN, 1 + LAT_NN * LAT_NN,
+                             1 + LAT_NN + LAT_NN * LAT_NN, LAT_NN + LAT_NN * LAT_NN};
+  std::vector<char> cell(LAT_N * LAT_N * LAT_N, 0);
+  for (int32_t k = k0; k < k1; ++k) {
+    const int32_t* nodes = conn + (int64_t)key[k].second * 8;
+    int p[8];
+    for (int a = 0; a < 8; ++a)
+      p[a] = lat[std::lower_bound(ids.begin(), ids.end(), nodes[a]) - ids.begin()];
+    const int ix = p[0] % LAT_NN, iy = (p[0] / LAT_NN) % LAT_NN, iz = p[0] / (LAT_NN * LAT_NN);
+    if (ix >= LAT_N || iy >= LAT_N || iz >= LAT_N) return false;
+    for (int a = 1; a < 8; ++a)
+      if (p[a] != p[0] + off[a]) return false;
+    char& c = cell[ix + LAT_N * (iy + LAT_N * iz)];
+    if (c) return false;
+    c = 1;
+  }
   return true;
 }
 
@@ -455,16 +521,39 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
         hi[d] = std::max(hi[d], s);
       }
     const double bits = (dim == 3) ? 2097151.0 : 2147483647.0;
+    // Centroids on a tensor grid (a structured mesh, any spacing per axis): quantize by
+    // grid index, so that runs of 8^dim Morton keys are aligned 8 x 8 (x 8) cubes.
+    std::vector<double> axis[3];
+    bool grid = n_elems > 0;
+    {
+      int64_t cells = 1;
+      for (int d = 0; d < dim && grid; ++d) {
+        axis[d].resize(n_elems);
+        for (int64_t e = 0; e < n_elems; ++e) axis[d][e] = cen[e * dim + d];
+        std::sort(axis[d].begin(), axis[d].end());
+        axis[d].erase(std::unique(axis[d].begin(), axis[d].end()), axis[d].end());
+        cells *= (int64_t)axis[d].size();
+        if (cells > n_elems || (double)axis[d].size() > bits) grid = false;
+      }
+      grid = grid && cells == n_elems;
+    }
     for (int64_t e = 0; e < n_elems; ++e) {
       uint64_t code = 0;
       for (int d = 0; d < dim; ++d) {
-        const double w = hi[d] - lo[d];
-        const double t = w > 0 ? (cen[e * dim + d] - lo[d]) / w : 0.0;
-        const uint64_t qd = (uint64_t)(t * bits);
+        uint64_t qd;
+        if (grid) {
+          qd = (uint64_t)(std::lower_bound(axis[d].begin(), axis[d].end(), cen[e * dim + d]) -
+                          axis[d].begin());
+        } else {
+          const double w = hi[d] - lo[d];
+          const double t = w > 0 ? (cen[e * dim + d] - lo[d]) / w : 0.0;
+          qd = (uint64_t)(t * bits);
+        }
         code |= (dim == 3 ? spread3(qd) : spread2(qd)) << d;
       }
       key[e] = {code, (int32_t)e};
     }
+    for (auto& a : axis) std::vector<double>().swap(a);
     cen.clear();
     cen.shrink_to_fit();
     std::sort(key.begin(), key.end());
@@ -503,10 +592,10 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
     const int32_t nb = (int32_t)blk_nodes.size();
     P->n_blocks = nb;
     if (elem == TG_HEX8 && dim == 3 && nb > 0) {
-      // 2: all boxes, 1: all parallelepipeds, 0: general
+      // 3: 8 x 8 x 8 box lattice, 2: all boxes, 1: all parallelepipeds, 0: general
       std::vector<char> kind(nb, 2);
       parallel_for(nb, [&](int64_t b0, int64_t b1, int) {
-        for (int64_t b = b0; b < b1; ++b)
+        for (int64_t b = b0; b < b1; ++b) {
           for (int32_t k = P->blk_elem_ptr[b]; k < P->blk_elem_ptr[b + 1] && kind[b]; ++k) {
             const int32_t* nodes = conn + (int64_t)key[k].second * npe;
             if (!(hex_affine_exact<double>(coords, nodes) && hex_affine_exact<float>(coords, nodes)))
@@ -515,11 +604,16 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
                      !(hex_box_exact<double>(coords, nodes) && hex_box_exact<float>(coords, nodes)))
               kind[b] = 1;
           }
+          if (kind[b] == 2 &&
+              hex_block_lattice(coords, conn, key, P->blk_elem_ptr[b], P->blk_elem_ptr[b + 1]))
+            kind[b] = 3;
+        }
       });
       std::vector<int32_t> order;
-      for (int want = 2; want >= 0; --want) {
+      for (int want = 3; want >= 0; --want) {
         for (int32_t b = 0; b < nb; ++b)
           if (kind[b] == want) order.push_back(b);
+        if (want == 3) P->n_lattice = (int32_t)order.size();
         if (want == 2) P->n_diag = (int32_t)order.size();
         if (want == 1) P->n_affine = (int32_t)order.size();
       }
@@ -571,6 +665,12 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
           }
         }
         std::sort(ids.begin(), ids.end());
+        if (b < P->n_lattice) {  // local node = grid position i + 9 j + 81 k
+          std::vector<int32_t> lat, by_lat(ids.size());
+          lattice_positions(coords, ids, lat);
+          for (size_t l = 0; l < ids.size(); ++l) by_lat[lat[l]] = ids[l];
+          ids.swap(by_lat);
+        }
         const int32_t n0 = P->blk_node_ptr[b];
         for (size_t l = 0; l < ids.size(); ++l) lid[ids[l]] = (int32_t)l;
         // colouring in Morton order
@@ -705,6 +805,7 @@ extern "C" int tg_plan_sizes(const void* handle, int64_t* s) {
   s[9] = P->n_affine;
   s[10] = P->n_diag;
   s[11] = P->max_elems;
+  s[12] = P->n_lattice;
   return TG_OK;
 }
 

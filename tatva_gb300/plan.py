@@ -37,9 +37,9 @@ class BlockPlan:
                                    xyz.ctypes.data, xyz.shape[1], self.block_elems,
                                    self.max_local_nodes, ctypes.byref(h)))
         try:
-            sizes = np.zeros(12, dtype=np.int64)
+            sizes = np.zeros(13, dtype=np.int64)
             _lib.check(L.tg_plan_sizes(h, sizes.ctypes.data))
-            nb, ne, ncol, nloc, nsh, npart, maxl, maxc, npad, naff, ndiag, maxe = (
+            nb, ne, ncol, nloc, nsh, npart, maxl, maxc, npad, naff, ndiag, maxe, nlat = (
                 int(x) for x in sizes)
             host = {
                 "blk_elem_ptr": np.zeros(nb + 1, np.int32),
@@ -65,7 +65,7 @@ class BlockPlan:
         self.sizes = dict(n_blocks=nb, n_elems=ne, color_ofs=ncol, local_nodes=nloc,
                           n_shared=nsh, n_partials=npart, max_local_nodes=maxl,
                           max_block_colors=maxc, stride=npad, n_affine_blocks=naff,
-                          n_diag_blocks=ndiag, max_block_elems=maxe)
+                          n_diag_blocks=ndiag, max_block_elems=maxe, n_lattice_blocks=nlat)
         self.device = torch.device(device)
         self.dev = {k: torch.from_numpy(v).to(self.device) for k, v in host.items()}
         s = _lib.BlockPlan()
@@ -75,8 +75,11 @@ class BlockPlan:
         s.n_affine_blocks = naff
         s.n_diag_blocks = ndiag
         s.max_block_elems = maxe
+        s.n_lattice_blocks = nlat
         for k in order:
             setattr(s, k, self.dev[k].data_ptr())
+        if np.array_equal(host["shared_slots"][:npart], np.arange(npart, dtype=np.int32)):
+            s.shared_slots = None  # identity: the reduce reads partials in slot order
         self.struct = s
         self.box_geom32 = None
         if elem_id == _lib.TG_HEX8 and ndiag > 0 and self.device.type == "cuda":

@@ -67,7 +67,7 @@ int main(void) {
   /* plan on the host, then to the device */
   void* h = NULL;
   TG(tg_plan_build(TG_HEX8, conn, ne, nn, X, 3, 512, 4096, &h));
-  int64_t sz[12];
+  int64_t sz[13];
   TG(tg_plan_sizes(h, sz));
   const int64_t nb = sz[0], nel = sz[1], ncol = sz[2], nloc = sz[3], nsh = sz[4], npart = sz[5];
   int32_t *bep = malloc(4 * (nb + 1)), *bcp = malloc(4 * (nb + 1)), *cof = malloc(4 * (ncol + 1));
@@ -88,6 +88,7 @@ int main(void) {
   p.n_affine_blocks = (int32_t)sz[9];
   p.n_diag_blocks = (int32_t)sz[10];
   p.max_block_elems = (int32_t)sz[11];
+  p.n_lattice_blocks = (int32_t)sz[12];
   p.blk_elem_ptr = dcopy(bep, 4 * (nb + 1));
   p.blk_color_ptr = dcopy(bcp, 4 * (nb + 1));
   p.color_ofs = dcopy(cof, 4 * ncol);

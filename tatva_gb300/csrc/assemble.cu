@@ -621,6 +621,9 @@ template <class T, int V, int MODE>
 __global__ void shared_reduce_kernel(const tg_block_plan p, const T* __restrict__ partials,
                                      const T* __restrict__ v, const uint8_t* __restrict__ fixed,
                                      T* __restrict__ y) {
+  // launched as a programmatic dependent of the block kernel: wait until that grid has
+  // finished and its partial sums are visible (no-op for an ordinary launch)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= p.n_shared) return;
   const int64_t g = p.shared_node[s];
@@ -1060,9 +1063,21 @@ extern "C" int tg_apply(int elem, int prec, int mode, const tg_material* mat,
             }
             TG_TRY(launch_check("tg_apply: block kernel"));
             if (plan->n_shared > 0) {
-              shared_reduce_kernel<T, C::V, MODE><<<grid_for(plan->n_shared, 256), 256, 0, st>>>(
-                  *plan, (const T*)workspace, (const T*)v, fixed, (T*)y);
-              TG_TRY(launch_check("tg_apply: shared reduce"));
+              // programmatic dependent launch: the reduce grid is set up while the block
+              // kernel drains, and its griddepcontrol.wait orders it after that kernel
+              cudaLaunchConfig_t cfg = {};
+              cfg.gridDim = dim3((unsigned)grid_for(plan->n_shared, 256));
+              cfg.blockDim = dim3(256);
+              cfg.dynamicSmemBytes = 0;
+              cfg.stream = st;
+              cudaLaunchAttribute attr[1];
+              attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+              attr[0].val.programmaticStreamSerializationAllowed = 1;
+              cfg.attrs = attr;
+              cfg.numAttrs = 1;
+              TG_TRY(cuda_check(cudaLaunchKernelEx(&cfg, shared_reduce_kernel<T, C::V, MODE>, *plan,
+                                                   (const T*)workspace, (const T*)v, fixed, (T*)y),
+                                "tg_apply: shared reduce"));
             }
             return TG_OK;
           });

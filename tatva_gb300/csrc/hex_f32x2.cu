@@ -548,6 +548,7 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
     if (bi + 2 * stride < nblk) issue_cofs(b + 2 * stride, s);
     cp_async_commit();
   }
+  asm volatile("griddepcontrol.launch_dependents;");
   cp_async_wait0();
 }
 
@@ -815,6 +816,7 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
     if (bi + 2 * stride < nblk) issue_meta(bi + 2 * stride, s);
     cp_async_commit();
   }
+  asm volatile("griddepcontrol.launch_dependents;");
   cp_async_wait0();
 }
 

@@ -565,10 +565,16 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
 // connectivity: a block reads its 729 node ids and partial slots, the input vector at
 // those nodes and the 27 coordinates of its grid lines.
 constexpr int LT_THREADS = 128;
-constexpr int LT_NODES = 729, LT_RING = 732, LT_MERGE = 153;
-// W [2][729] float4 | merge parts [4][153] float4 | ids [2][732] | slots [2][732] |
+constexpr int LT_NODES = 729, LT_RING = 732, LT_MERGE = 153, LT_PARTS = 81;
+// W [2][729] float4 | merge parts [4 warps][81] float4 | ids [2][732] | slots [2][732] |
 // grid lines [2][32]
-constexpr size_t LT_SMEM = (2 * LT_NODES + 4 * LT_MERGE) * 16 + 4 * LT_RING * 4 + 2 * 32 * 4;
+constexpr size_t LT_SMEM = (2 * LT_NODES + 4 * LT_PARTS) * 16 + 4 * LT_RING * 4 + 2 * 32 * 4;
+
+// Index of node (ni, nj, L) among the 81 merge parts of warp (jh, kh): row j = 4 at the
+// warp's layers 4 kh .. 4 kh + 4 first (45), then layer 4 at the warp's other rows (36).
+__host__ __device__ __forceinline__ int lt_part(int jh, int kh, int ni, int nj, int L) {
+  return (nj == 4) ? ni + 9 * (L - 4 * kh) : 45 + ni + 9 * (jh == 0 ? nj : nj - 5);
+}
 
 __device__ __forceinline__ void cp_async_wait1() {
   asm volatile("cp.async.wait_group 1;" ::: "memory");
@@ -583,7 +589,7 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
   extern __shared__ __align__(16) float sm[];
   float4* const W = reinterpret_cast<float4*>(sm);
   float4* const Pm = W + 2 * LT_NODES;
-  int* const ids = reinterpret_cast<int*>(Pm + 4 * LT_MERGE);
+  int* const ids = reinterpret_cast<int*>(Pm + 4 * LT_PARTS);
   int* const slots = ids + 2 * LT_RING;
   float* const geo = reinterpret_cast<float*>(slots + 2 * LT_RING);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -593,6 +599,7 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
   // node ids and partial slots of block b into ring entry r
   auto issue_meta = [&](int b, int r) {
     const int64_t n0 = nbase + (int64_t)LT_NODES * b;
+#pragma unroll 3
     for (int l = tid; l < LT_NODES; l += LT_THREADS) {
       cp_async4(ids + r * LT_RING + l, p.lnode_gid + n0 + l);
       cp_async4(slots + r * LT_RING + l, p.lnode_slot + n0 + l);
@@ -605,9 +612,11 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
     float* Wr = reinterpret_cast<float*>(W + r * LT_NODES);
     const int* id = ids + r * LT_RING;
     const int sub = lane / 3, d = lane - 3 * sub;
-    if (lane < 24)
+    if (lane < 24) {
+#pragma unroll 4
       for (int l = warp * 8 + sub; l < LT_NODES; l += 32)
         cp_async4(Wr + l * 4 + d, fin + (int64_t)id[l] * 3 + d);
+    }
     if (tid < 27) {
       const int a = tid / 9, q = tid - 9 * a;
       const int l = a == 0 ? q : (a == 1 ? 9 * q : 81 * q);
@@ -669,8 +678,7 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
     // warp also touches the node
     auto put = [&](int ni, int nj, int L, const float (&v)[3]) {
       if (nj == 4 || L == 4) {
-        const int m = (nj == 4) ? ni + 9 * L : 81 + ni + 9 * (nj < 4 ? nj : nj - 1);
-        Pm[warp * LT_MERGE + m] = make_float4(v[0], v[1], v[2], 0.f);
+        Pm[warp * LT_PARTS + lt_part(jh, kh, ni, nj, L)] = make_float4(v[0], v[1], v[2], 0.f);
       } else {
         emit(ni + 9 * nj + 81 * L, v[0], v[1], v[2]);
       }
@@ -696,9 +704,31 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
         }
       }
       put(i, j, L, Q[0]);
-      if (i == 7) put(8, j, L, Q[1]);
-      if (jl == 3) put(i, j + 1, L, Q[2]);
-      if (i == 7 && jl == 3) put(8, j + 1, L, Q[3]);
+      // the warp's 13 halo nodes in one pass: (8, j) from lanes i = 7, (i, j + 1) from
+      // lanes jl = 3, and lane 31's second and third halo nodes handed to lanes 0, 1
+      float X2[3], X3[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        X2[c] = __shfl_sync(0xffffffffu, Q[2][c], 31);
+        X3[c] = __shfl_sync(0xffffffffu, Q[3][c], 31);
+      }
+      const int jt = 4 * jh + 4;
+      int hi_ = -1, hj = 0;
+      float hv[3];
+      if (i == 7) {
+        hi_ = 8; hj = j;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) hv[c] = Q[1][c];
+      } else if (jl == 3) {
+        hi_ = i; hj = jt;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) hv[c] = Q[2][c];
+      } else if (lane < 2) {
+        hi_ = 7 + lane; hj = jt;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) hv[c] = lane == 0 ? X2[c] : X3[c];
+      }
+      if (hi_ >= 0) put(hi_, hj, L, hv);
     };
     auto load_layer = [&](int L, float (&o)[4][3]) {
 #pragma unroll
@@ -798,16 +828,20 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
         nj = jj < 4 ? jj : jj + 1;
         L = 4;
       }
-      if (nj == 4 && L == 4) {
-        const float4 a0 = Pm[m], a1 = Pm[LT_MERGE + m], a2 = Pm[2 * LT_MERGE + m],
-                     a3 = Pm[3 * LT_MERGE + m];
+      if (nj == 4 && L == 4) {  // all four warps, in warp order
+        const float4 a0 = Pm[lt_part(0, 0, ni, 4, 4)];
+        const float4 a1 = Pm[LT_PARTS + lt_part(1, 0, ni, 4, 4)];
+        const float4 a2 = Pm[2 * LT_PARTS + lt_part(0, 1, ni, 4, 4)];
+        const float4 a3 = Pm[3 * LT_PARTS + lt_part(1, 1, ni, 4, 4)];
         a = make_float4(((a0.x + a1.x) + a2.x) + a3.x, ((a0.y + a1.y) + a2.y) + a3.y,
                         ((a0.z + a1.z) + a2.z) + a3.z, 0.f);
       } else {
-        // row j = 4: warps (jh 0, jh 1) of the layer's half; layer 4: warps (kh 0, kh 1)
-        const int w0 = (nj == 4) ? 2 * (L < 4 ? 0 : 1) : (nj < 4 ? 0 : 1);
-        const int w1 = (nj == 4) ? w0 + 1 : w0 + 2;
-        const float4 a0 = Pm[w0 * LT_MERGE + m], a1 = Pm[w1 * LT_MERGE + m];
+        // row j = 4: warps jh = 0, 1 of the layer's half; layer 4: warps kh = 0, 1 of
+        // the row's half
+        const int kh0 = (nj == 4) ? (L < 4 ? 0 : 1) : 0, kh1 = (nj == 4) ? kh0 : 1;
+        const int jh0 = (nj == 4) ? 0 : (nj < 4 ? 0 : 1), jh1 = (nj == 4) ? 1 : jh0;
+        const float4 a0 = Pm[(jh0 + 2 * kh0) * LT_PARTS + lt_part(jh0, kh0, ni, nj, L)];
+        const float4 a1 = Pm[(jh1 + 2 * kh1) * LT_PARTS + lt_part(jh1, kh1, ni, nj, L)];
         a = make_float4(a0.x + a1.x, a0.y + a1.y, a0.z + a1.z, 0.f);
       }
       emit(ni + 9 * nj + 81 * L, a.x, a.y, a.z);

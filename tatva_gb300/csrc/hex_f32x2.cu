@@ -567,8 +567,9 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
 constexpr int LT_THREADS = 128;
 constexpr int LT_NODES = 729, LT_RING = 732, LT_MERGE = 153, LT_PARTS = 81;
 // W [2][729] float4 | merge parts [4 warps][81] float4 | ids [2][732] | slots [2][732] |
-// grid lines [2][32]
-constexpr size_t LT_SMEM = (2 * LT_NODES + 4 * LT_PARTS) * 16 + 4 * LT_RING * 4 + 2 * 32 * 4;
+// grid lines [2][32] | Dirichlet bits of the current block's nodes [732] bytes
+constexpr size_t LT_SMEM =
+    (2 * LT_NODES + 4 * LT_PARTS) * 16 + 4 * LT_RING * 4 + 2 * 32 * 4 + LT_RING;
 
 // Index of node (ni, nj, L) among the 81 merge parts of warp (jh, kh): row j = 4 at the
 // warp's layers 4 kh .. 4 kh + 4 first (45), then layer 4 at the warp's other rows (36).
@@ -592,6 +593,7 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
   int* const ids = reinterpret_cast<int*>(Pm + 4 * LT_PARTS);
   int* const slots = ids + 2 * LT_RING;
   float* const geo = reinterpret_cast<float*>(slots + 2 * LT_RING);
+  uint8_t* const fbits = reinterpret_cast<uint8_t*>(geo + 2 * 32);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = p.n_lattice_blocks, stride = gridDim.x;
   const int64_t nbase = __ldg(p.blk_node_ptr);
@@ -644,13 +646,30 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
     const float4* Ws = W + s * LT_NODES;
     const int* id = ids + s * LT_RING;
     const int* sl = slots + s * LT_RING;
-    if (MODE == TG_MODE_HVP && fixed) {
+    if (fixed) {
+      // the block's Dirichlet bits into shared memory (read once per node here, not at
+      // every emission); HVP: fixed inputs read as 0
       float* Wf = reinterpret_cast<float*>(W + s * LT_NODES);
-      for (int l = tid; l < LT_NODES; l += LT_THREADS) {
-        const int64_t g = id[l];
+      constexpr int NQ = (LT_NODES + LT_THREADS - 1) / LT_THREADS;
+      uint8_t f[NQ][3];  // all of this thread's mask bytes in flight at once
 #pragma unroll
-        for (int d = 0; d < 3; ++d)
-          if (fixed[g * 3 + d]) Wf[l * 4 + d] = 0.f;
+      for (int qn = 0; qn < NQ; ++qn) {
+        const int l = tid + qn * LT_THREADS;
+        const int64_t g = l < LT_NODES ? id[l] : 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) f[qn][d] = l < LT_NODES ? fixed[g * 3 + d] : 0;
+      }
+#pragma unroll
+      for (int qn = 0; qn < NQ; ++qn) {
+        const int l = tid + qn * LT_THREADS;
+        if (l >= LT_NODES) continue;
+        const int m = (f[qn][0] != 0) | (f[qn][1] != 0) << 1 | (f[qn][2] != 0) << 2;
+        fbits[l] = (uint8_t)m;
+        if (MODE == TG_MODE_HVP && m) {
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            if (m >> d & 1) Wf[l * 4 + d] = 0.f;
+        }
       }
       __syncthreads();
     }
@@ -662,11 +681,12 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
       const int q = sl[l];
       const float v[3] = {v0, v1, v2};
       if (q < 0) {
+        const int m = fixed ? fbits[l] : 0;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const int64_t dof = g * 3 + d;
           float val = v[d];
-          if (fixed && fixed[dof]) val = (MODE == TG_MODE_HVP) ? vin[dof] : 0.f;
+          if (m >> d & 1) val = (MODE == TG_MODE_HVP) ? vin[dof] : 0.f;
           y[dof] = val;
         }
       } else {

@@ -55,29 +55,55 @@ struct DotAcc<double> {
 };
 
 // ------------------------------------------------------------------ reductions
+// Sum of one value per thread of the CTA into out[k] (thread 0 writes): a fixed tree
+// (shuffles inside each warp, then the warps' sums in warp order), so the result does
+// not depend on timing.  Ends with a barrier: the CTA may call it again.
 template <int K>
 __device__ __forceinline__ void block_reduce_store(double (&v)[K], double* __restrict__ out) {
-  __shared__ double sh[K][DOT_THREADS];
+  constexpr int NW = DOT_THREADS / 32;
+  __shared__ double sh[K][NW];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < K; ++k) sh[k][threadIdx.x] = v[k];
-  __syncthreads();
-  for (int s = DOT_THREADS / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
+  for (int k = 0; k < K; ++k) {
 #pragma unroll
-      for (int k = 0; k < K; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
-    }
-    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (lane == 0) sh[k][warp] = v[k];
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) out[k] = sh[k][0];
+    for (int k = 0; k < K; ++k) {
+      double a = sh[k][0];
+#pragma unroll
+      for (int w = 1; w < NW; ++w) a += sh[k][w];
+      out[k] = a;
+    }
   }
+  __syncthreads();
 }
 
-// Chunk count of the fixed partition of an n-vector: one chunk per 2048 entries, at
-// most DOT_CHUNKS (small vectors launch few CTAs; the count depends on n only).
+// Called by every thread after thread 0 stored this CTA's partials: true in the CTA
+// that arrives last, which then sees every CTA's partials (read them with __ldcg).
+// That CTA resets the ticket for the next launch.  An arrival counter, no waiting.
+__device__ __forceinline__ bool last_cta(unsigned* ticket) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+    if (last) *ticket = 0u;
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// Chunk count of the fixed partition of an n-vector: one chunk per 8192 entries, at
+// most DOT_CHUNKS (about five CTAs per SM for the largest vectors here, one wave; the
+// count depends on n only).
 __host__ __device__ inline int dot_chunks(int64_t n) {
-  const int64_t c = (n + 2047) / 2048;
+  const int64_t c = (n + 8191) / 8192;
   return (int)(c < 1 ? 1 : (c > DOT_CHUNKS ? DOT_CHUNKS : c));
 }
 
@@ -116,6 +142,7 @@ __global__ void __launch_bounds__(DOT_THREADS)
   chunk_range(n, i0, i1);
   const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
   DotAcc<T> acc;
+#pragma unroll 4
   for (int64_t i = i0 + 4 * threadIdx.x; i < iv; i += 4 * DOT_THREADS) {
     T a[4], b[4];
     ldv(x + i, a);
@@ -212,11 +239,18 @@ __global__ void csr_dirichlet_kernel(int64_t n_rows, const int32_t* __restrict__
 }
 
 // ------------------------------------------------------------------ CG kernels
-// z = r / diag, p = z, partials of (r.z, r.r)
+// dinv = 1 / diag (once per restart: the iterations multiply)
+template <class T>
+__global__ void inv_kernel(int64_t n, const T* __restrict__ diag, T* __restrict__ dinv) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dinv[i] = T(1) / diag[i];
+}
+
+// p = z = r dinv, partials of (r.z, r.r)
 template <class T>
 __global__ void __launch_bounds__(DOT_THREADS)
-    cg_init_kernel(int64_t n, const T* __restrict__ r, const T* __restrict__ diag,
-                   T* __restrict__ z, T* __restrict__ p, double* __restrict__ part) {
+    cg_init_kernel(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv,
+                   T* __restrict__ p, double* __restrict__ part) {
   int64_t i0, i1;
   chunk_range(n, i0, i1);
   const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
@@ -224,20 +258,18 @@ __global__ void __launch_bounds__(DOT_THREADS)
   for (int64_t i = i0 + 4 * threadIdx.x; i < iv; i += 4 * DOT_THREADS) {
     T rr[4], dd[4], zz[4];
     ldv(r + i, rr);
-    ldv(diag + i, dd);
+    ldv(dinv + i, dd);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      zz[k] = rr[k] / dd[k];
-      a0.add(rr[k], zz[k]);
-      a1.add(rr[k], rr[k]);
-    }
-    stv(z + i, zz);
+    for (int k = 0; k < 4; ++k) zz[k] = rr[k] * dd[k];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a0.add(rr[k], zz[k]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a1.add(rr[k], rr[k]);
     stv(p + i, zz);
   }
   for (int64_t i = iv + threadIdx.x; i < i1; i += DOT_THREADS) {
     const T ri = r[i];
-    const T zi = ri / diag[i];
-    z[i] = zi;
+    const T zi = ri * dinv[i];
     p[i] = zi;
     a0.add(ri, zi);
     a1.add(ri, ri);
@@ -264,14 +296,32 @@ __global__ void cg_init_final_kernel(const double* __restrict__ part, double* __
   }
 }
 
+// partials of p.q; the last CTA adds them (fixed order) and sets
 // alpha = rz / pq (breakdown flag on pq <= 0 or non-finite)
-__global__ void cg_alpha_kernel(const double* __restrict__ part, double* __restrict__ scal,
-                                int nchunks) {
-  double v[1] = {0.0};
-  for (int b = threadIdx.x; b < nchunks; b += DOT_THREADS) v[0] += part[b];
+template <class T>
+__global__ void __launch_bounds__(DOT_THREADS)
+    cg_pq_kernel(const T* __restrict__ p, const T* __restrict__ q, int64_t n,
+                 double* __restrict__ part, double* __restrict__ scal, unsigned* ticket) {
+  int64_t i0, i1;
+  chunk_range(n, i0, i1);
+  const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
+  DotAcc<T> acc;
+#pragma unroll 4
+  for (int64_t i = i0 + 4 * threadIdx.x; i < iv; i += 4 * DOT_THREADS) {
+    T a[4], b[4];
+    ldv(p + i, a);
+    ldv(q + i, b);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc.add(a[k], b[k]);
+  }
+  for (int64_t i = iv + threadIdx.x; i < i1; i += DOT_THREADS) acc.add(p[i], q[i]);
+  double v[1] = {acc.value()};
+  block_reduce_store<1>(v, part + blockIdx.x);
+  if (!last_cta(ticket)) return;
+  double w[1] = {0.0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += DOT_THREADS) w[0] += __ldcg(part + b);
   __shared__ double out[1];
-  block_reduce_store<1>(v, out);
-  __syncthreads();
+  block_reduce_store<1>(w, out);
   if (threadIdx.x == 0) {
     const double pq = out[0];
     scal[SCAL_PQ] = pq;
@@ -281,61 +331,56 @@ __global__ void cg_alpha_kernel(const double* __restrict__ part, double* __restr
   }
 }
 
-// x += alpha p; r -= alpha q; z = r/diag; partials of (r.z, r.r)
+// x += alpha p; r -= alpha q; partials of (r.z, r.r) with z = r dinv; the last CTA
+// adds them (fixed order) and sets beta = rz_new / rz, rz = rz_new, rr
 template <class T>
 __global__ void __launch_bounds__(DOT_THREADS)
-    cg_update_kernel(int64_t n, const double* __restrict__ scal, T* __restrict__ x,
-                     T* __restrict__ r, T* __restrict__ z, const T* __restrict__ p,
-                     const T* __restrict__ q, const T* __restrict__ diag,
-                     double* __restrict__ part) {
+    cg_update_kernel(int64_t n, double* __restrict__ scal, T* __restrict__ x,
+                     T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
+                     const T* __restrict__ dinv, double* __restrict__ part, unsigned* ticket) {
   int64_t i0, i1;
   chunk_range(n, i0, i1);
   const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
   const T alpha = (T)scal[SCAL_ALPHA];
   DotAcc<T> a0, a1;
+#pragma unroll 2
   for (int64_t i = i0 + 4 * threadIdx.x; i < iv; i += 4 * DOT_THREADS) {
     T xx[4], pp[4], rr[4], qq[4], dd[4], zz[4];
     ldv(x + i, xx);
     ldv(p + i, pp);
     ldv(r + i, rr);
     ldv(q + i, qq);
-    ldv(diag + i, dd);
+    ldv(dinv + i, dd);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       xx[k] += alpha * pp[k];
       rr[k] = rr[k] - alpha * qq[k];
-      zz[k] = rr[k] / dd[k];
-      a0.add(rr[k], zz[k]);
-      a1.add(rr[k], rr[k]);
+      zz[k] = rr[k] * dd[k];
     }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a0.add(rr[k], zz[k]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a1.add(rr[k], rr[k]);
     stv(x + i, xx);
     stv(r + i, rr);
-    stv(z + i, zz);
   }
   for (int64_t i = iv + threadIdx.x; i < i1; i += DOT_THREADS) {
     x[i] += alpha * p[i];
     const T ri = r[i] - alpha * q[i];
     r[i] = ri;
-    const T zi = ri / diag[i];
-    z[i] = zi;
-    a0.add(ri, zi);
+    a0.add(ri, ri * dinv[i]);
     a1.add(ri, ri);
   }
   double v[2] = {a0.value(), a1.value()};
   block_reduce_store<2>(v, part + 2 * blockIdx.x);
-}
-
-// beta = rz_new / rz; rz = rz_new; rr stored
-__global__ void cg_beta_kernel(const double* __restrict__ part, double* __restrict__ scal,
-                               int nchunks) {
-  double v[2] = {0.0, 0.0};
-  for (int b = threadIdx.x; b < nchunks; b += DOT_THREADS) {
-    v[0] += part[2 * b];
-    v[1] += part[2 * b + 1];
+  if (!last_cta(ticket)) return;
+  double w[2] = {0.0, 0.0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += DOT_THREADS) {
+    w[0] += __ldcg(part + 2 * b);
+    w[1] += __ldcg(part + 2 * b + 1);
   }
   __shared__ double out[2];
-  block_reduce_store<2>(v, out);
-  __syncthreads();
+  block_reduce_store<2>(w, out);
   if (threadIdx.x == 0) {
     const double rz_new = out[0];
     const bool bad = scal[SCAL_FLAG] != 0.0 || !isfinite(rz_new);
@@ -346,20 +391,22 @@ __global__ void cg_beta_kernel(const double* __restrict__ part, double* __restri
   }
 }
 
+// p = r dinv + beta p
 template <class T>
-__global__ void cg_p_kernel(int64_t n, const double* __restrict__ scal, const T* __restrict__ z,
-                            T* __restrict__ p) {
+__global__ void cg_p_kernel(int64_t n, const double* __restrict__ scal, const T* __restrict__ r,
+                            const T* __restrict__ dinv, T* __restrict__ p) {
   const int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   const T beta = (T)scal[SCAL_BETA];
   if (i + 3 < n) {
-    T zz[4], pp[4];
-    ldv(z + i, zz);
+    T rr[4], dd[4], pp[4];
+    ldv(r + i, rr);
+    ldv(dinv + i, dd);
     ldv(p + i, pp);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) pp[k] = zz[k] + beta * pp[k];
+    for (int k = 0; k < 4; ++k) pp[k] = rr[k] * dd[k] + beta * pp[k];
     stv(p + i, pp);
   } else {
-    for (int64_t j = i; j < n; ++j) p[j] = z[j] + beta * p[j];
+    for (int64_t j = i; j < n; ++j) p[j] = r[j] * dinv[j] + beta * p[j];
   }
 }
 
@@ -511,8 +558,9 @@ extern "C" int tg_operator_apply(const tg_operator_desc* op, const void* x, void
 namespace tg {
 
 struct CgBuffers {
-  void *r, *z, *p, *q, *apply_ws;
+  void *r, *p, *q, *dinv, *apply_ws;
   double *part, *scal;
+  unsigned* ticket;  // [2] last-CTA arrival counters of the p.q and update kernels
   size_t apply_bytes;
 };
 
@@ -520,7 +568,8 @@ static size_t cg_bytes(const tg_operator_desc* op) {
   const int64_t n = op_ndofs(op);
   const size_t vs = align256((size_t)n * prec_size(op->prec));
   return 4 * vs + align256(tg_operator_workspace_bytes(op)) +
-         align256(DOT_CHUNKS * 2 * sizeof(double)) + align256(SCAL_N * sizeof(double));
+         align256(DOT_CHUNKS * 2 * sizeof(double)) + align256(SCAL_N * sizeof(double)) +
+         align256(2 * sizeof(unsigned));
 }
 
 static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
@@ -529,26 +578,29 @@ static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
   CgBuffers b;
   const size_t vb = (size_t)n * prec_size(op->prec);
   b.r = c.take(vb);
-  b.z = c.take(vb);
   b.p = c.take(vb);
+  b.dinv = c.take(vb);
   b.q = c.take(vb);
   b.apply_bytes = tg_operator_workspace_bytes(op);
   b.apply_ws = c.take(b.apply_bytes);
   b.part = (double*)c.take(DOT_CHUNKS * 2 * sizeof(double));
   b.scal = (double*)c.take(SCAL_N * sizeof(double));
+  b.ticket = (unsigned*)c.take(2 * sizeof(unsigned));
   return b;
 }
 
-// r = b - A x ; z = r/diag ; p = z ; scal <- (rz, rr)
+// dinv = 1/diag ; r = b - A x ; p = r dinv ; scal <- (rz, rr); arrival counters zeroed
 template <class T>
 static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* diag,
                       CgBuffers& B, cudaStream_t st) {
   const int64_t n = op_ndofs(op);
   TG_TRY(tg_operator_apply(op, x, B.r, B.apply_ws, B.apply_bytes, st));
   axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
-  cg_init_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, (const T*)B.r, diag, (T*)B.z,
+  inv_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, diag, (T*)B.dinv);
+  cg_init_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, (const T*)B.r, (const T*)B.dinv,
                                                         (T*)B.p, B.part);
   cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
+  TG_TRY(cuda_check(cudaMemsetAsync(B.ticket, 0, 2 * sizeof(unsigned), st), "cg: counters"));
   return launch_check("cg restart");
 }
 
@@ -557,14 +609,13 @@ static int cg_iteration(const tg_operator_desc* op, T* x, const T* diag, CgBuffe
                         cudaStream_t st) {
   const int64_t n = op_ndofs(op);
   TG_TRY(tg_operator_apply(op, B.p, B.q, B.apply_ws, B.apply_bytes, st));
-  dot_partial_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n,
-                                                            B.part);
-  cg_alpha_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
-  cg_update_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, B.scal, x, (T*)B.r, (T*)B.z,
-                                                          (const T*)B.p, (const T*)B.q, diag,
-                                                          B.part);
-  cg_beta_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
-  cg_p_kernel<T><<<grid_for((n + 3) / 4, 256), 256, 0, st>>>(n, B.scal, (const T*)B.z, (T*)B.p);
+  cg_pq_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n, B.part,
+                                                      B.scal, B.ticket);
+  cg_update_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, B.scal, x, (T*)B.r,
+                                                          (const T*)B.p, (const T*)B.q,
+                                                          (const T*)B.dinv, B.part, B.ticket + 1);
+  cg_p_kernel<T><<<grid_for((n + 3) / 4, 256), 256, 0, st>>>(n, B.scal, (const T*)B.r,
+                                                          (const T*)B.dinv, (T*)B.p);
   return launch_check("cg iteration");
 }
 

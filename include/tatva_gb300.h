@@ -321,6 +321,20 @@ TG_API int tg_set_column(int prec, const void* col, int64_t n, int n_colors, int
 /* y = A x, CSR (int32 indptr/indices), data/x/y of precision prec */
 TG_API int tg_spmv(int prec, int64_t n_rows, const int32_t* indptr, const int32_t* indices,
             const void* data, const void* x, void* y, void* stream);
+/* Node blocks of a CSR matrix with 3 dofs per node (pattern_from_mesh with
+ * n_dofs_per_node = 3, dof = 3 node + c, sparse/_extraction.py:57-60): the three rows
+ * of node i list the same neighbour nodes, each as 3 consecutive columns.  Writes
+ * node_ptr[n_rows/3 + 1] and node_indices[nnz/9] (neighbour node ids); sets the
+ * device int *not_blocked to 1 if the pattern has another form (leaves it otherwise).
+ * Device buffers; n_rows must be a multiple of 3.                               */
+TG_API int tg_csr_node_blocks3(int64_t n_rows, const int32_t* indptr, const int32_t* indices,
+                               int32_t* node_ptr, int32_t* node_indices, int32_t* not_blocked,
+                               void* stream);
+/* y = A x over the node blocks of tg_csr_node_blocks3: reads one neighbour id per
+ * 3 x 3 block instead of one column index per entry; data stays in CSR order.   */
+TG_API int tg_spmv_blocks3(int prec, int64_t n_rows, const int32_t* indptr,
+                           const int32_t* node_ptr, const int32_t* node_indices,
+                           const void* data, const void* x, void* y, void* stream);
 /* CSR diagonal (Jacobi) */
 TG_API int tg_csr_diagonal(int prec, int64_t n_rows, const int32_t* indptr, const int32_t* indices,
                     const void* data, void* diag, void* stream);
@@ -360,6 +374,10 @@ typedef struct tg_operator_desc {
   const int32_t* csr_indptr;
   const int32_t* csr_indices;
   const void* csr_data;  /* precision prec */
+  /* optional node blocks of the CSR pattern (tg_csr_node_blocks3); when both are
+   * set the SpMV is tg_spmv_blocks3                                              */
+  const int32_t* csr_node_ptr;
+  const int32_t* csr_node_indices;
 } tg_operator_desc;
 
 /* Dirichlet rows/columns of an assembled matrix: for fixed rows data = (col == row);

@@ -119,6 +119,8 @@ class OperatorDesc(ctypes.Structure):
         ("csr_indptr", c_void_p),
         ("csr_indices", c_void_p),
         ("csr_data", c_void_p),
+        ("csr_node_ptr", c_void_p),
+        ("csr_node_indices", c_void_p),
     ]
 
 
@@ -163,6 +165,8 @@ SIGNATURES = {
     "tg_color_seeds": (I, [I, P, L, I, I, P, P]),
     "tg_set_column": (I, [I, P, L, I, I, P, P]),
     "tg_spmv": (I, [I, L, P, P, P, P, P, P]),
+    "tg_csr_node_blocks3": (I, [L, P, P, P, P, P, P]),
+    "tg_spmv_blocks3": (I, [I, L, P, P, P, P, P, P, P]),
     "tg_csr_diagonal": (I, [I, L, P, P, P, P, P]),
     "tg_csr_apply_dirichlet": (I, [I, L, P, P, P, P, P]),
     "tg_operator_workspace_bytes": (S, [P]),

@@ -211,6 +211,71 @@ __global__ void spmv_kernel(int64_t n_rows, const int32_t* __restrict__ indptr,
   if (live && lane == 0) y[row] = acc;
 }
 
+// node blocks of a 3-dof-per-node CSR pattern: one thread per node (the last thread
+// writes node_ptr[n_nodes]); any row triple not of the blocked form raises the flag
+__global__ void node_blocks3_kernel(int64_t n_nodes, const int32_t* __restrict__ indptr,
+                                    const int32_t* __restrict__ indices,
+                                    int32_t* __restrict__ nptr, int32_t* __restrict__ nidx,
+                                    int32_t* __restrict__ not_blocked) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n_nodes) return;
+  const int32_t r0 = indptr[3 * i];
+  if (r0 % 9 != 0) {
+    *not_blocked = 1;
+    return;
+  }
+  nptr[i] = r0 / 9;
+  if (i == n_nodes) return;
+  const int32_t L = indptr[3 * i + 1] - r0;
+  bool good = (L % 3 == 0) && (indptr[3 * i + 2] - indptr[3 * i + 1] == L) &&
+              (indptr[3 * i + 3] - indptr[3 * i + 2] == L);
+  for (int32_t m = 0; good && m < L / 3; ++m) {
+    const int32_t j3 = indices[r0 + 3 * m];
+    good = (j3 % 3 == 0);
+    for (int a = 0; good && a < 3; ++a)
+      for (int b = 0; b < 3; ++b) good = good && indices[r0 + a * L + 3 * m + b] == j3 + b;
+    if (good) nidx[r0 / 9 + m] = j3 / 3;
+  }
+  if (!good) *not_blocked = 1;
+}
+
+// y = A x over node blocks: SPMV_LANES lanes per node, each lane a strided subset of
+// the node's neighbour blocks, the three row sums reduced over the lanes in a fixed tree
+template <class T>
+__global__ void spmv_blocks3_kernel(int64_t n_nodes, const int32_t* __restrict__ indptr,
+                                    const int32_t* __restrict__ nptr,
+                                    const int32_t* __restrict__ nidx, const T* __restrict__ data,
+                                    const T* __restrict__ x, T* __restrict__ y) {
+  const int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / SPMV_LANES;
+  const int lane = threadIdx.x & (SPMV_LANES - 1);
+  const bool live = node < n_nodes;
+  T s0 = T(0), s1 = T(0), s2 = T(0);
+  if (live) {
+    const int32_t b0 = __ldg(nptr + node), deg = __ldg(nptr + node + 1) - b0;
+    const int64_t r0 = __ldg(indptr + 3 * node);
+    const int64_t L = 3 * (int64_t)deg;
+    for (int32_t m = lane; m < deg; m += SPMV_LANES) {
+      const int64_t j = __ldg(nidx + b0 + m);
+      const T x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+      const T* v = data + r0 + 3 * m;
+      s0 += __ldg(v) * x0 + __ldg(v + 1) * x1 + __ldg(v + 2) * x2;
+      s1 += __ldg(v + L) * x0 + __ldg(v + L + 1) * x1 + __ldg(v + L + 2) * x2;
+      s2 += __ldg(v + 2 * L) * x0 + __ldg(v + 2 * L + 1) * x1 + __ldg(v + 2 * L + 2) * x2;
+    }
+  }
+#pragma unroll
+  for (int o = SPMV_LANES / 2; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o, SPMV_LANES);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o, SPMV_LANES);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o, SPMV_LANES);
+  }
+  if (live && lane == 0) {
+    y[3 * node] = s0;
+    y[3 * node + 1] = s1;
+    y[3 * node + 2] = s2;
+  }
+}
+
 template <class T>
 __global__ void csr_diag_kernel(int64_t n_rows, const int32_t* __restrict__ indptr,
                                 const int32_t* __restrict__ indices, const T* __restrict__ data,
@@ -469,6 +534,39 @@ extern "C" int tg_spmv(int prec, int64_t n_rows, const int32_t* indptr, const in
   });
 }
 
+extern "C" int tg_csr_node_blocks3(int64_t n_rows, const int32_t* indptr, const int32_t* indices,
+                                   int32_t* node_ptr, int32_t* node_indices, int32_t* not_blocked,
+                                   void* stream) {
+  if (n_rows < 0 || n_rows % 3 != 0) return set_error(TG_ERR_VALUE, "n_rows must be a multiple of 3");
+  TG_TRY(check_ptr(indptr, "indptr"));
+  TG_TRY(check_ptr(node_ptr, "node_ptr"));
+  TG_TRY(check_ptr(not_blocked, "not_blocked"));
+  const int64_t nn = n_rows / 3;
+  node_blocks3_kernel<<<grid_for(nn + 1, 256), 256, 0, as_stream(stream)>>>(
+      nn, indptr, indices, node_ptr, node_indices, not_blocked);
+  return launch_check("tg_csr_node_blocks3");
+}
+
+extern "C" int tg_spmv_blocks3(int prec, int64_t n_rows, const int32_t* indptr,
+                               const int32_t* node_ptr, const int32_t* node_indices,
+                               const void* data, const void* x, void* y, void* stream) {
+  if (n_rows < 0 || n_rows % 3 != 0) return set_error(TG_ERR_VALUE, "n_rows must be a multiple of 3");
+  if (n_rows == 0) return TG_OK;
+  TG_TRY(check_ptr(indptr, "indptr"));
+  TG_TRY(check_ptr(node_ptr, "node_ptr"));
+  TG_TRY(check_ptr(node_indices, "node_indices"));
+  TG_TRY(check_ptr(data, "data"));
+  TG_TRY(check_ptr(x, "x"));
+  TG_TRY(check_ptr(y, "y"));
+  const int64_t nn = n_rows / 3;
+  return dispatch_prec(prec, [&](auto t) -> int {
+    using T = decltype(t);
+    spmv_blocks3_kernel<T><<<grid_for(nn * SPMV_LANES, 256), 256, 0, as_stream(stream)>>>(
+        nn, indptr, node_ptr, node_indices, (const T*)data, (const T*)x, (T*)y);
+    return launch_check("tg_spmv_blocks3");
+  });
+}
+
 extern "C" int tg_csr_diagonal(int prec, int64_t n_rows, const int32_t* indptr,
                                const int32_t* indices, const void* data, void* diag,
                                void* stream) {
@@ -547,9 +645,13 @@ extern "C" size_t tg_operator_workspace_bytes(const tg_operator_desc* op) {
 extern "C" int tg_operator_apply(const tg_operator_desc* op, const void* x, void* y,
                                  void* workspace, size_t workspace_bytes, void* stream) {
   TG_TRY(check_ptr(op, "op"));
-  if (op->csr_data)
+  if (op->csr_data) {
+    if (op->csr_node_ptr && op->csr_node_indices)
+      return tg_spmv_blocks3(op->prec, op->n_rows, op->csr_indptr, op->csr_node_ptr,
+                             op->csr_node_indices, op->csr_data, x, y, stream);
     return tg_spmv(op->prec, op->n_rows, op->csr_indptr, op->csr_indices, op->csr_data, x, y,
                    stream);
+  }
   return tg_apply(op->elem, op->prec, TG_MODE_HVP, &op->mat, op->plan, op->coords, op->n_nodes,
                   op->u, x, op->fixed, y, workspace, workspace_bytes, stream);
 }

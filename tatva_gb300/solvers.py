@@ -8,7 +8,8 @@ These wrappers drive the native solvers of the C ABI:
                 FP64 dot products), ``tg_cg_solve``
 * ``mixed_cg``  FP32 HVP + FP32 CG inner solves with FP64 iterative refinement on the
                 true residual (FP64 HVP), ``tg_mixed_solve``
-* ``csr_cg``    CG on an assembled CSR matrix (``tg_spmv``)
+* ``csr_cg``    CG on an assembled CSR matrix (``tg_spmv``; ``tg_spmv_blocks3`` for
+  3-dof-per-node patterns)
 * ``newton``    load-stepped Newton: FP64 residual and update, colored sparse tangent
                 (``sparse.jacfwd`` of the residual, optionally in FP32), CSR CG inner solve
 
@@ -20,6 +21,7 @@ from __future__ import annotations
 
 import ctypes
 import time
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -130,6 +132,33 @@ def mixed_cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None,
                        message=msg)
 
 
+# id of a pattern's indices tensor -> (weak reference to it, node blocks or None)
+_BLOCKS3: dict = {}
+
+
+def node_blocks3(cm):
+    """Node blocks of a 3-dof-per-node CSR pattern (``tg_csr_node_blocks3``), computed
+    once per pattern (per indices tensor); None when the pattern is not of that form."""
+    hit = _BLOCKS3.get(id(cm.indices))
+    if hit is not None and hit[0]() is cm.indices:
+        return hit[1]
+    for k in [k for k, (ref, _) in _BLOCKS3.items() if ref() is None]:
+        del _BLOCKS3[k]
+    n, nnz = cm.shape[0], cm.nnz
+    res = None
+    if n > 0 and n % 3 == 0 and nnz % 9 == 0:
+        dev = cm.indices.device
+        nptr = torch.empty(n // 3 + 1, dtype=torch.int32, device=dev)
+        nidx = torch.empty(max(nnz // 9, 1), dtype=torch.int32, device=dev)
+        flag = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("tg_csr_node_blocks3", n, ptr(cm.indptr), ptr(cm.indices), ptr(nptr),
+                  ptr(nidx), ptr(flag), torch.cuda.current_stream(dev).cuda_stream)
+        if int(flag.item()) == 0:
+            res = (nptr, nidx)
+    _BLOCKS3[id(cm.indices)] = (weakref.ref(cm.indices), res)
+    return res
+
+
 def csr_cg(cm, b: torch.Tensor, x0=None, *, fixed=None, rtol: float = 1e-8,
            maxiter: int = 100000, check_every: int = 50, raise_on_fail: bool = True,
            apply_dirichlet: bool = True) -> SolveResult:
@@ -157,6 +186,9 @@ def csr_cg(cm, b: torch.Tensor, x0=None, *, fixed=None, rtol: float = 1e-8,
     desc.n_rows = n
     desc.csr_indptr, desc.csr_indices, desc.csr_data = (cm.indptr.data_ptr(),
                                                         cm.indices.data_ptr(), data.data_ptr())
+    blocks = node_blocks3(cm)
+    if blocks is not None:  # 3 dofs per node: one neighbour id per 3 x 3 block
+        desc.csr_node_ptr, desc.csr_node_indices = blocks[0].data_ptr(), blocks[1].data_ptr()
     nb = _lib.lib().tg_cg_workspace_bytes(ctypes.byref(desc))
     ws = workspace(nb, b.device)
 

@@ -456,3 +456,38 @@ def test_periodic_reduced_residual_and_hessian(cuda):
     Ko = omat.assemble_dense(oo, Ke, 1)
     Kro = P.T.toarray() @ Ko @ P.toarray()
     assert np.abs(Kr.toarray() - Kro).max() / np.abs(Kro).max() < F64_TOL
+
+
+def test_spmv_node_blocks3(cuda):
+    """SpMV over the node blocks of a 3-dof-per-node pattern equals the row-CSR SpMV
+    (FP64: same products, other summation order); a pattern of another form is
+    reported as not blocked."""
+    from tatva_gb300 import _lib, solvers
+    from tatva_gb300._device import ptr
+
+    c, e = om.kuhn_box((1, 1, 1), (6, 5, 4), origin=(0, 0, 0))
+    pat = osp.pattern_from_mesh(c, e, 3)
+    cm = sparse.ColoredMatrix.from_csr(pat, device=cuda)
+    rng = np.random.default_rng(2)
+    data = torch.as_tensor(rng.standard_normal(cm.nnz), device=cuda)
+    x = torch.as_tensor(rng.standard_normal(cm.shape[0]), device=cuda)
+    blocks = solvers.node_blocks3(cm)
+    assert blocks is not None
+    st = torch.cuda.current_stream().cuda_stream
+    y_csr, y_blk = torch.empty_like(x), torch.empty_like(x)
+    _lib.call("tg_spmv", _lib.TG_F64, cm.shape[0], ptr(cm.indptr), ptr(cm.indices), ptr(data),
+              ptr(x), ptr(y_csr), st)
+    _lib.call("tg_spmv_blocks3", _lib.TG_F64, cm.shape[0], ptr(cm.indptr), ptr(blocks[0]),
+              ptr(blocks[1]), ptr(data), ptr(x), ptr(y_blk), st)
+    A = pat.astype(np.float64)
+    A.data = data.cpu().numpy()
+    assert rel(y_blk, A @ x.cpu().numpy()) < F64_TOL
+    assert rel(y_blk, y_csr) < F64_TOL
+    # 6 rows of 3 entries (nnz 18) whose row triples differ: not blocked
+    import scipy.sparse as sps
+
+    rows = np.repeat(np.arange(6), 3)
+    cols = (rows + np.tile(np.arange(3), 6)) % 6
+    pat2 = sps.csr_matrix((np.ones(18), (rows, cols)), shape=(6, 6))
+    pat2.sort_indices()
+    assert solvers.node_blocks3(sparse.ColoredMatrix.from_csr(pat2, device=cuda)) is None

@@ -533,7 +533,8 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
         std::sort(axis[d].begin(), axis[d].end());
         axis[d].erase(std::unique(axis[d].begin(), axis[d].end()), axis[d].end());
         cells *= (int64_t)axis[d].size();
-        if (cells > n_elems || (double)axis[d].size() > bits) grid = false;
+        // the per-axis counts of a tensor grid multiply to n_elems
+        if (cells > n_elems || n_elems % cells != 0 || (double)axis[d].size() > bits) grid = false;
       }
       grid = grid && cells == n_elems;
     }

@@ -394,6 +394,13 @@ def bench_newton(dev, args):
     P = stretched_kuhn(n, dev)
     en, c = P["energy"], P["coords"]
     cm = sparse.ColoredMatrix.from_csr(sparse.pattern_from_mesh(P["mesh"], 3), device=dev)
+    # warm-up, untimed: one Newton iteration of the first load step builds the element
+    # plan and loads every kernel of the loop (lazily loaded kernels cost seconds on
+    # first use after other large work in the process)
+    lifter0 = Lifter(en.n_dofs, Fixed(P["dofs"], P["values"](0.2 / steps)))
+    u0 = torch.zeros(en.n_dofs, dtype=torch.float64, device=dev)
+    solvers.newton(en, lifter0.lift(lifter0.reduce(u0), u0), lifter0, colored_matrix=cm,
+                   rtol=1e-10, max_iter=1)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
     u = torch.zeros(en.n_dofs, dtype=torch.float64, device=dev)

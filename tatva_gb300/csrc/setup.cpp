@@ -558,7 +558,11 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
     cen.clear();
     cen.shrink_to_fit();
     std::sort(key.begin(), key.end());
-    // 2. chunk into blocks (element count and local-node cap)
+    // 2. chunk into blocks (element count and local-node cap).  On a 3-D tensor grid
+    // with 512-element blocks, a block also ends where the 8 x 8 x 8 Morton cube changes
+    // (key >> 9), so that every full cube is one block whatever the grid's sides, and
+    // the partial cubes at the far faces form blocks of their own.
+    const bool cube_cuts = grid && dim == 3 && block_elems == 512;
     std::vector<int32_t> stamp(n_nodes, -1);
     P->blk_elem_ptr.push_back(0);
     std::vector<int32_t> blk_nodes;  // local node count per block
@@ -569,7 +573,8 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
         int add = 0;  // upper bound on the nodes this element brings into block b
         for (int a = 0; a < npe; ++a)
           if (stamp[conn[(int64_t)e * npe + a]] != b) ++add;
-        if (ne > 0 && (ne >= block_elems || nl + add > max_local_nodes)) {
+        const bool new_cube = cube_cuts && k > 0 && (key[k].first >> 9) != (key[k - 1].first >> 9);
+        if (ne > 0 && (ne >= block_elems || nl + add > max_local_nodes || new_cube)) {
           P->blk_elem_ptr.push_back((int32_t)k);
           blk_nodes.push_back(nl);
           ++b;

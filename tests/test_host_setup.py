@@ -196,3 +196,30 @@ def test_synthetic_request_stream():
     assert 0.8 < (len(arr) - 1) / arr[-1] / 2000.0 < 1.2
     assert {r.side for r in reqs} == {16, 24, 32, 48, 64}
     assert all(0.2 <= r.poisson <= 0.45 for r in reqs)
+
+
+@pytest.mark.parametrize("shape,n_lat,n_blocks", [((16, 16, 16), 8, 8), ((20, 20, 20), 8, 27),
+                                                   ((24, 16, 8), 6, 6), ((12, 12, 12), 1, 8)])
+def test_lattice_blocks_of_structured_bricks(shape, n_lat, n_blocks):
+    """Structured bricks (any spacing per axis): every full 8 x 8 x 8 cube of cells is
+    one lattice block, local nodes in grid order l = i + 9 j + 81 k; other cells form
+    blocks of their own.  Node numbering does not matter; a moved node does."""
+    rng = np.random.default_rng(0)
+    c, e = om.brick(*shape, lengths=tuple(float(s) for s in shape))
+    for d in range(3):  # uneven spacing per axis
+        lines = np.cumsum(np.r_[0.0, 0.5 + rng.random(shape[d])])
+        c[:, d] = lines[np.rint(c[:, d]).astype(int)]
+    perm = rng.permutation(c.shape[0])
+    c, e = c[perm], np.argsort(perm)[e]
+    p = BlockPlan(_lib.TG_HEX8, e, c, "cpu", block_elems=512, threads=128)
+    assert p.sizes["n_lattice_blocks"] == n_lat and p.sizes["n_blocks"] == n_blocks
+    bnp, gid = p.host["blk_node_ptr"], p.host["lnode_gid"]
+    for b in range(n_lat):
+        x = c[gid[bnp[b]:bnp[b + 1]]].reshape(9, 9, 9, 3)  # [k][j][i]
+        assert np.all(np.diff(x[..., 0], axis=2) > 0) and np.all(np.diff(x[..., 1], axis=1) > 0)
+        assert np.all(np.diff(x[..., 2], axis=0) > 0)
+        assert np.all(x[..., 0] == x[0, 0, :, 0]) and np.all(x[..., 2] == x[:, :1, :1, 2])
+    c2 = c.copy()
+    c2[np.argmin(np.linalg.norm(c2 - c2.mean(axis=0), axis=1))] += 0.01
+    p2 = BlockPlan(_lib.TG_HEX8, e, c2, "cpu", block_elems=512, threads=128)
+    assert p2.sizes["n_lattice_blocks"] < max(n_lat, 1)

@@ -125,10 +125,10 @@ def test_lattice_mixed_with_general_blocks(cuda):
 def test_lattice_many_blocks_per_cta_and_bitwise_repeat(cuda):
     """More lattice blocks than resident CTAs (each CTA walks several blocks through
     the double-buffered pipeline); two calls give the same bits."""
-    c, e = om.brick(64, 64, 32)
+    c, e = om.brick(128, 64, 64)  # 1024 blocks, above the 608 resident CTAs of a GB300
     op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
     plan = op.plan(512, 4096, 128)
-    assert plan.sizes["n_lattice_blocks"] == plan.sizes["n_blocks"] == 256
+    assert plan.sizes["n_lattice_blocks"] == plan.sizes["n_blocks"] == 1024
     en = materials.LinearElastic(op, 0.7, 1.9)
     en.use_plan(plan)
     g = torch.Generator(device=cuda).manual_seed(1)
@@ -137,3 +137,20 @@ def test_lattice_many_blocks_per_cta_and_bitwise_repeat(cuda):
     assert torch.equal(a, b)
     y64 = en.hvp(None, v.double())
     assert rel(a, y64) < F32_TOL
+
+
+def test_lattice_and_box_blocks_on_uneven_sides(cuda):
+    """Sides that are not multiples of 8: the full 8 x 8 x 8 cubes run the lattice kernel,
+    the partial cubes the colour-ordered box kernel, in the same HVP."""
+    rng = np.random.default_rng(7)
+    shape = (20, 12, 10)
+    c, e = om.brick(*shape, lengths=tuple(float(s) for s in shape))
+    for d in range(3):
+        lines = np.cumsum(np.r_[0.0, 0.5 + rng.random(shape[d])])
+        c[:, d] = lines[np.rint(c[:, d]).astype(int)]
+    plan, v, u, y, r, y0, r0 = _run(c, e, cuda)
+    assert plan.sizes["n_lattice_blocks"] == 2
+    assert plan.sizes["n_diag_blocks"] == plan.sizes["n_blocks"] > 2
+    yo, ro = _oracle(c, e, v, u)
+    assert rel(y, yo) < F32_TOL and rel(r, ro) < F32_TOL
+    assert rel(y, y0) < SWAP_TOL and rel(r, r0) < SWAP_TOL

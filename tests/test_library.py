@@ -91,3 +91,17 @@ def test_lifter_semantics_on_host():
     np.testing.assert_array_equal(
         lf2.lift_from_zeros(torch.zeros(4, dtype=torch.float64)).numpy(), [0, 0, 0, 0, 0, 1])
     assert lf2.fixed_mask("cpu").tolist() == [1, 0, 0, 0, 0, 1]
+
+
+def test_node_block_spmv_argument_checks():
+    """The node-block entry points reject row counts that are not multiples of 3 and
+    missing buffers before any launch."""
+    L = _lib.lib()
+    with pytest.raises(ValueError, match="multiple of 3"):
+        _lib.check(L.tg_csr_node_blocks3(4, None, None, None, None, None, None))
+    with pytest.raises(ValueError, match="multiple of 3"):
+        _lib.check(L.tg_spmv_blocks3(_lib.TG_F32, 5, None, None, None, None, None, None, None))
+    with pytest.raises(ValueError):
+        _lib.check(L.tg_spmv_blocks3(_lib.TG_F32, 6, None, None, None, None, None, None, None))
+    assert L.tg_spmv_blocks3(_lib.TG_F32, 0, None, None, None, None, None, None, None) == _lib.TG_OK
+

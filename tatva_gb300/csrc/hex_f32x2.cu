@@ -1,6 +1,9 @@
 // FP32 linear-elastic Hex8 residual / HVP on blocks of exact parallelepipeds:
 // persistent CTAs, cp.async pipeline, two elements per thread in packed f32x2
-// arithmetic.
+// arithmetic.  Two kernels: hex_le_f32x2_kernel (any box / parallelepiped block,
+// colour-ordered shared-memory accumulation, described here) and
+// hex_le_lattice_kernel (blocks that are 8 x 8 x 8 grids of boxes: register and
+// lane-shuffle accumulation, described above its definition further down).
 //
 // Same mathematics, plan and summation order as the modal path of assemble.cu (the
 // 2x2x2 Gauss sum evaluated exactly in the monomial basis of grad u through an

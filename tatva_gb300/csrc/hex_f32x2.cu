@@ -774,7 +774,8 @@ __global__ void __launch_bounds__(LT_THREADS, 4)
     for (int t = 0; t < 4; ++t)
 #pragma unroll
       for (int c = 0; c < 3; ++c) C[t][c] = 0.f;
-#pragma unroll 1
+    // both pair steps in one scheduling region (measured 3 % faster than a loop)
+#pragma unroll
     for (int ps = 0; ps < 2; ++ps) {
       const int k = k0 + 2 * ps;
       float mid[4][3], top[4][3];

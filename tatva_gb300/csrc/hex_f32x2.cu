@@ -564,9 +564,11 @@ __global__ void __launch_bounds__(P6_THREADS, KIND == P6_AFFINE ? 3 : 4)
 // elements is formed in registers (the layer carried up the sweep) and by lane shuffles
 // (along i, then along j) in a fixed order; the 153 nodes that two or four warps touch
 // (row j = 4 and layer k = 4) go through shared memory and are added in warp order
-// after the sweep.  No element colouring, no barrier inside the sweep, no element
-// connectivity: a block reads its 729 node ids and partial slots, the input vector at
-// those nodes and the 27 coordinates of its grid lines.
+// after the sweep.  No element colouring and no element connectivity: a block reads
+// its 729 node ids and partial slots, the input vector at those nodes and the 27
+// coordinates of its grid lines.  Barriers per block: data landed, mid-sweep (the next
+// block's ids landed: start its input gather), merge parts in place, ring free (plus
+// one after staging the Dirichlet bits when there is a mask).
 constexpr int LT_THREADS = 128;
 constexpr int LT_NODES = 729, LT_RING = 732, LT_MERGE = 153, LT_PARTS = 81;
 // W [2][729] float4 | merge parts [4 warps][81] float4 | ids [2][732] | slots [2][732] |

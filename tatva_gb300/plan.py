@@ -16,7 +16,9 @@ from . import _lib
 
 # Defaults measured on GB300 (HVP, graph-timed): Tri3 Poisson 1024^2 best at 2048 / 256,
 # Kuhn Tet4 96^3 at 2048 / 128 (34 colours per block: fewer threads keep more of them
-# busy in each colour pass), Hex8 box bricks at 512 elements per block.
+# busy in each colour pass), Hex8 box bricks at 512 elements per block -- on structured
+# bricks each full 8 x 8 x 8 cube of cells is then a lattice block (sizes
+# "n_lattice_blocks"), which the FP32 linear-elastic kernels sum without colouring.
 DEFAULT_BLOCK_ELEMS = {_lib.TG_TRI3: 2048, _lib.TG_TET4: 2048, _lib.TG_HEX8: 512}
 DEFAULT_THREADS = {_lib.TG_TRI3: 256, _lib.TG_TET4: 128, _lib.TG_HEX8: 128}
 DEFAULT_MAX_LOCAL = 4096

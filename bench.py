@@ -1,28 +1,38 @@
-"""Benchmark: Hex8 linear-elastic Hessian-vector product on a 128^3 brick.
+"""Benchmark: Hex8 linear-elastic solve to FP64 relative residual 1e-10 on a 128^3 brick.
 
 Workload (the reference's Hex8 configuration): structured Hex8 brick 128x128x128
 (2,097,152 elements, 2,146,689 nodes, 6,440,067 dofs), 2x2x2 Gauss, E = 1.0,
 nu = 0.3, clamped x = 0 face, uniform normal traction 1e-3 on x = 1.
 
-* step: one matrix-free HVP y = K v over the whole mesh (FP32 kernel, FP32
-  vectors and coordinates), inputs resident in HBM; the L2 is flushed (256 MiB
-  write) before every step and the HVP -- captured once as a CUDA graph of its two
-  kernel launches and replayed -- is timed with CUDA events on its stream.
-* value: dofs per second (GDOF/s) over the K timed steps, summed over ranks.
-* e2e: the same HVP through the public API with the input copied from pinned host
-  memory and the result copied back inside the timed region, every step; the copies
-  of neighbouring steps overlap the HVP (three streams, double buffers).  The fully
-  sequential figure is reported beside it.
-* solve: the Jacobi-CG solve of the same problem to true FP64 relative residual
-  1e-10, plain FP64 vs mixed FP32/FP64 (iterative refinement); solves/s of each.
-* roofline: algorithmic bytes per HVP (x read + y written + int32 connectivity +
-  coordinates: 2*4*N_dof + 4*8*E + 4*3*N_nodes = 144.39 MB) over the measured HVP
-  time, against the measured HBM copy bandwidth.
-* cpu_baseline: the numpy restatement (oracle) of the same HVP on a 32^3 brick.
+* step: one Jacobi-preconditioned CG solve of that system from x = 0 to
+  ||b - A x|| <= 1e-10 ||b||, the residual evaluated in FP64.  The solve is the
+  mixed-precision one of the public API (``solvers.mixed_cg``): FP32 matrix-free HVP
+  and inner CG vectors, FP64 true residual, refinement update and dot products.
+  The L2 is flushed (256 MiB write) before every solve; the solve's own working set
+  (about 280 MB of vectors) is larger than the L2 anyway.
+* value: solves per second over the K timed solves (CUDA events on the solver's
+  stream), summed over ranks (replicas).
+* e2e: the same solve through the public API with the right-hand side copied from
+  pinned host memory and the solution copied back inside the timed region.
+* roofline: the solve's dominant kernel, the FP32 HVP (captured once as a CUDA graph
+  and replayed with the L2 flushed before every launch): algorithmic bytes per HVP
+  (x read + y written + int32 connectivity + coordinates: 2*4*N_dof + 4*8*E +
+  4*3*N_nodes = 144.39 MB) over its measured time, against the measured HBM copy
+  bandwidth; ``traffic`` is the HVP's DRAM bytes per launch from the committed ncu
+  summary of the same kernels.
+* extras: the plain FP64 Jacobi-CG solve of the same system (the reference user's
+  algorithm, on the GPU), FP32 and FP64 HVP rates, the batched Poisson solve, the
+  request loop and the Neo-Hookean Newton run.
+* cpu_baseline: the numpy restatement (oracle) of one FP64 Jacobi-CG iteration on the
+  same 128^3 system over all host cores, times the FP64 solver's iteration count.
+
+``--impl reference`` times the same CPU restatement of the FP64 Jacobi-CG iteration
+(the reference itself needs JAX, which is not installable here) on the same 128^3
+system and reports solves/s = 1 / (seconds per iteration x iterations to 1e-10).
+``--driver NAME`` runs one of the workload drivers that the ncu summaries under
+profiles/ were taken on (see ``run_driver``).
 
 Multi-GPU: replicas only (each rank runs the same workload on its own GPU).
-``--impl reference`` times the CPU restatement of the HVP on all host cores
-(the reference itself needs JAX, which is not installable here).
 """
 
 from __future__ import annotations
@@ -40,9 +50,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "Hex8 HVP GDOF/s"
-UNIT = "GDOF/s"
+METRIC = "Hex8 HVP GDOF/s; solves/s & p99 latency at rel-res 1e-10, mixed vs FP64"
+UNIT = "solves/s"
 N_CELLS = 128
+RTOL = 1e-10
+# Jacobi-CG iterations that the FP64 solver needs on the clamped 128^3 brick to reach
+# rel-res 1e-10 (tg_cg_solve, measured on GB300 with convergence checks every 10
+# iterations).  The CPU arm runs the same FP64 algorithm, so it needs the same count;
+# timing the whole CPU solve (hours) is replaced by iterations x seconds per iteration.
+FP64_CG_ITERATIONS = {128: 1000}
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "hex8_hvp_f32_brick128_traffic.md")
+
+
+def workload_config(n: int) -> dict:
+    """The config block both arms print (identical, so the arms can be matched)."""
+    return {"workload": f"hex8 linear elasticity, structured brick {n}^3 ({n ** 3} elements, "
+                        f"{3 * (n + 1) ** 3} dofs), 2x2x2 Gauss, E=1 nu=0.3, clamped x=0, "
+                        "traction 1e-3 on x=1; Jacobi-CG solve to FP64 rel-res 1e-10",
+            "cells_per_side": n, "dofs": 3 * (n + 1) ** 3, "rtol": RTOL}
 
 
 def _peaks():
@@ -54,24 +79,17 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_from_profile():
-    """Per-launch DRAM bytes of the HVP kernels from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "hex8_hvp_f32_brick.md")
-    if not os.path.exists(p):
+def _profile_value(path, key):
+    """``key: value`` line of a committed ncu summary, or None."""
+    if not os.path.exists(path):
         return None
-    for line in open(p):
-        if line.startswith("traffic_bytes_per_hvp_128:"):
+    for line in open(path):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip().split()[0])
             except ValueError:
                 return None
     return None
-
-
-def brick_problem(n, device):
-    from tatva_gb300.problems import clamped_brick
-
-    return clamped_brick(n, device, traction=1e-3)
 
 
 class ClockSampler:
@@ -133,107 +151,408 @@ def _dist():
     return ws, rank, local
 
 
-class CpuHvp:
-    """Oracle (numpy, FP64) HVP of the same law on an n^3 brick, optionally with the
-    elements split over a pool of worker processes (spawned once)."""
+# ----------------------------------------------------------------------------- CPU arm
+class CpuBrickCg:
+    """FP64 Jacobi-CG on the clamped n^3 brick with the oracle (numpy) HVP, the
+    elements split into contiguous layers over a pool of spawned worker processes.
 
-    def __init__(self, n_cells=32, processes=1):
-        from oracle import elements as oe
+    The brick's elements are numbered layer by layer (k slowest), so each worker's
+    element range touches one contiguous slab of nodes.  Coordinates, connectivity and
+    the input vector are shared with the workers through shared memory; a worker
+    returns only its slab of the product."""
+
+    def __init__(self, n_cells: int, processes: int):
+        import multiprocessing as mp
+
         from oracle import materials as omat
         from oracle import mesh as om
-        from oracle import operator as oop
 
         c, e = om.brick(n_cells, n_cells, n_cells)
+        nn = c.shape[0]
+        self.ndof = 3 * nn
         mu, lm = omat.lame_from_young(1.0, 0.3)
-        self.law = omat.LinearElastic(mu, lm)
-        self.v = np.random.default_rng(0).standard_normal(c.shape[0] * 3)
-        self.ndof = c.shape[0] * 3
-        self.processes = processes
-        self.pool = None
-        if processes > 1:
-            import multiprocessing as mp
+        fixed = np.zeros(self.ndof, bool)
+        left = np.where(c[:, 0] == 0.0)[0]
+        for k in range(3):
+            fixed[left * 3 + k] = True
+        self.fixed = fixed
+        b = np.zeros(self.ndof)
+        h = 1.0 / n_cells
+        right = np.where(c[:, 0] == 1.0)[0]
+        jy = np.rint(c[right, 1] / h).astype(int)
+        jz = np.rint(c[right, 2] / h).astype(int)
+        mult = (np.where((jy == 0) | (jy == n_cells), 1, 2)
+                * np.where((jz == 0) | (jz == n_cells), 1, 2))
+        b[right * 3] = 1e-3 * (h * h / 4) * mult
+        self.b = b
+        self.processes = max(1, int(processes))
+        self.shm = {}
+        self.v = self._shared("v", np.zeros(self.ndof))
+        self._shared("c", c)
+        self._shared("e", e)
+        self.tasks = []
+        for ch in np.array_split(np.arange(e.shape[0]), self.processes):
+            e0, e1 = int(ch[0]), int(ch[-1]) + 1
+            lo, hi = int(e[e0:e1].min()), int(e[e0:e1].max()) + 1
+            self.tasks.append((e0, e1, lo, hi))
+        spec = {k: (m.name, a.shape, a.dtype.str) for k, (m, a) in self.shm.items()}
+        self.pool = mp.get_context("spawn").Pool(self.processes, initializer=_cpu_pool_init,
+                                                 initargs=(spec, mu, lm))
+        # Jacobi diagonal: element tangent diagonals of the law, summed per dof
+        diag = np.zeros(self.ndof)
+        for (lo, part) in self.pool.map(_cpu_pool_diag, self.tasks):
+            diag[3 * lo: 3 * lo + part.size] += part
+        self.dinv = np.where(fixed, 1.0, 1.0 / np.where(fixed, 1.0, diag))
 
-            self.chunks = np.array_split(np.arange(e.shape[0]), processes)
-            self.pool = mp.get_context("spawn").Pool(
-                processes, initializer=_pool_init, initargs=(c, e, self.law, self.v))
-        else:
-            self.op = oop.OracleOperator(c, e, oe.Hexahedron8())
+    def _shared(self, name, arr):
+        from multiprocessing import shared_memory
 
-    def step(self):
-        from oracle import materials as omat
+        m = shared_memory.SharedMemory(create=True, size=max(arr.nbytes, 1))
+        a = np.ndarray(arr.shape, dtype=arr.dtype, buffer=m.buf)
+        a[...] = arr
+        self.shm[name] = (m, a)
+        return a
 
-        if self.pool is not None:
-            return np.sum(self.pool.map(_pool_hvp, self.chunks), axis=0)
-        return omat.hvp(self.op, self.law, None, self.v)
+    def apply(self, p):
+        """A p with the Dirichlet rows of the identity (fixed inputs read as 0)."""
+        self.v[:] = np.where(self.fixed, 0.0, p)
+        y = np.zeros(self.ndof)
+        for (lo, part) in self.pool.map(_cpu_pool_hvp, self.tasks):
+            y[3 * lo: 3 * lo + part.size] += part
+        y[self.fixed] = p[self.fixed]
+        return y
 
-    def measure(self, min_seconds):
-        self.step()
-        reps, t0 = 0, time.perf_counter()
-        while True:
-            self.step()
-            reps += 1
-            if time.perf_counter() - t0 >= min_seconds:
-                break
-        dt = (time.perf_counter() - t0) / reps
-        return self.ndof / dt / 1e9, dt, reps
+    def start(self):
+        """CG state at x = 0: r = b, z = dinv r, p = z."""
+        self.x = np.zeros(self.ndof)
+        self.r = self.b.copy()
+        z = self.dinv * self.r
+        self.p = z
+        self.rz = float(self.r @ z)
+
+    def iteration(self):
+        q = self.apply(self.p)
+        alpha = self.rz / float(self.p @ q)
+        self.x += alpha * self.p
+        self.r -= alpha * q
+        z = self.dinv * self.r
+        rz = float(self.r @ z)
+        self.p = z + (rz / self.rz) * self.p
+        self.rz = rz
+
+    def time_iterations(self, warmup: int, steps: int) -> float:
+        self.start()
+        for _ in range(warmup):
+            self.iteration()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            self.iteration()
+        return (time.perf_counter() - t0) / max(steps, 1)
 
     def close(self):
-        if self.pool is not None:
-            self.pool.close()
-            self.pool.join()
+        self.pool.close()
+        self.pool.join()
+        for m, _ in self.shm.values():
+            m.close()
+            m.unlink()
+        self.shm = {}
 
 
-_POOL = {}
+_CPU = {}
 
 
-def _pool_init(c, e, law, v):
-    _POOL.update(c=c, e=e, law=law, v=v)
+def _cpu_pool_init(spec, mu, lm):
+    from multiprocessing import shared_memory
 
-
-def _pool_hvp(idx):
-    from oracle import elements as oe
     from oracle import materials as omat
+
+    arrs, keep = {}, []
+    for k, (name, shape, dt) in spec.items():
+        m = shared_memory.SharedMemory(name=name)
+        keep.append(m)
+        arrs[k] = np.ndarray(shape, dtype=np.dtype(dt), buffer=m.buf)
+    _CPU.update(arrs, keep=keep, law=omat.LinearElastic(mu, lm), ops={})
+
+
+def _cpu_op(task):
+    from oracle import elements as oe
     from oracle import operator as oop
 
-    c, e, law, v = _POOL["c"], _POOL["e"], _POOL["law"], _POOL["v"]
-    op = oop.OracleOperator(c, e[idx], oe.Hexahedron8())
-    return omat.hvp(op, law, None, v)
+    if task not in _CPU["ops"]:
+        e0, e1, lo, hi = task
+        _CPU["ops"][task] = oop.OracleOperator(_CPU["c"][lo:hi], _CPU["e"][e0:e1] - lo,
+                                               oe.Hexahedron8())
+    return _CPU["ops"][task]
+
+
+def _cpu_pool_diag(task):
+    """Diagonal of the linear-elastic element tangents, summed per dof:
+    K[(a,i),(a,i)] = sum_q w detJ (mu |grad N_a|^2 + (lambda + mu) (d_i N_a)^2)."""
+    op = _cpu_op(task)
+    law = _CPU["law"]
+    dNdX, detJ = op.geometry()  # (E,Q,3,n), (E,Q)
+    w = detJ * op.qw[None, :]
+    g2 = dNdX ** 2
+    de = (law.mu * np.einsum("eq,eqdn->en", w, g2)[:, :, None]
+          + (law.lmbda + law.mu) * np.einsum("eq,eqdn->end", w, g2))  # (E, n, 3)
+    lo, hi = task[2], task[3]
+    from oracle.operator import _scatter_add
+
+    return lo, _scatter_add(op.elements, de, hi - lo).reshape(-1)
+
+
+def _cpu_pool_hvp(task):
+    from oracle import materials as omat
+
+    op = _cpu_op(task)
+    lo, hi = task[2], task[3]
+    return lo, omat.hvp(op, _CPU["law"], None, _CPU["v"][3 * lo: 3 * hi])
 
 
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return
+    n = args.size
     cores = os.cpu_count() or 1
-    n = 48
-    cpu = CpuHvp(n, processes=cores)
-    ndof = cpu.ndof
-    for _ in range(args.warmup):
-        cpu.step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        cpu.step()
-    dt = (time.perf_counter() - t0) / args.steps
+    cpu = CpuBrickCg(n, cores)
+    sec = cpu.time_iterations(args.warmup, args.steps)
     cpu.close()
-    value = ndof / dt / 1e9
+    its = FP64_CG_ITERATIONS.get(n)
+    note = ""
+    if its is None:  # sizes without a measured count: the O(n) growth of Jacobi-CG
+        its = int(round(FP64_CG_ITERATIONS[N_CELLS] * n / N_CELLS))
+        note = " (iteration count scaled from the 128^3 measurement)"
+    solve_s = sec * its
+    value = 1.0 / solve_s
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ndof / value / 1e6,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": solve_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
-        "config": {"workload": f"hex8 linear-elastic HVP, structured brick {N_CELLS}^3 "
-                               f"({N_CELLS ** 3} elements, {3 * (N_CELLS + 1) ** 3} dofs), E=1 "
-                               "nu=0.3, 2x2x2 Gauss",
-                   "l2": "host CPU", "parallelism": "host cores",
-                   "step": f"one HVP over a {n}^3 sample brick of the workload"},
+        "data": "synthetic", "config": workload_config(n),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"numpy restatement of the HVP on a {n}^3 brick "
-                                   f"({ndof} dofs), elements split over {cores} processes"},
+                         "sample": f"numpy restatement of FP64 Jacobi-CG on the {n}^3 brick "
+                                   f"({cpu.ndof} dofs): {args.steps} timed iterations "
+                                   f"(HVP over {cores} processes, vectors in the parent) at "
+                                   f"{sec:.3f} s each, x {its} iterations to rel-res 1e-10"
+                                   + note},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference (JAX) cannot be installed offline; its CPU path is "
-                "represented by the numpy restatement of the same HVP",
+        "seconds_per_iteration": sec, "iterations_per_solve": its,
+        "note": "the reference (JAX) cannot be installed offline; its CPU path, "
+                "jax.scipy.sparse.linalg.cg with the jax.jvp(jax.grad(E)) HVP in FP64, is "
+                "represented by the numpy restatement of the same iteration",
     }
     print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def _hvp_timing(en, v, y, flush, steps, warmup, dev):
+    """Mean CUDA-event time (ms) of one HVP replayed from a CUDA graph, the L2 flushed
+    before every launch; events on the replaying stream."""
+    import torch
+
+    from tatva_gb300 import _lib
+
+    st = torch.cuda.current_stream(dev)
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(st)
+    with torch.cuda.stream(side):
+        en.apply(_lib.TG_MODE_HVP, None, v, out=y)
+    st.wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        en.apply(_lib.TG_MODE_HVP, None, v, out=y)
+    for _ in range(warmup):
+        flush.fill_(1.0)
+        graph.replay()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    for i in range(steps):
+        flush.fill_(float(i))
+        evs[i][0].record(st)
+        graph.replay()
+        evs[i][1].record(st)
+    torch.cuda.synchronize()
+    return float(np.mean([a.elapsed_time(b) for a, b in evs])), graph
+
+
+def run_ours(args):
+    import torch
+
+    from tatva_gb300 import autotune, replicas, solvers
+    from tatva_gb300.problems import clamped_brick
+
+    ws, rank, local = replicas.world()
+    torch.cuda.set_device(local)
+    replicas.init("nccl")
+    dev = torch.device("cuda", local)
+    n = args.size
+    P = clamped_brick(n, dev, traction=1e-3)
+    en = P["energy"]
+    ndof = en.n_dofs
+    tune = autotune.tune(en, dtype=torch.float32) if args.autotune else None
+    if not args.autotune and args.block_elems:
+        en.use_plan(P["op"].plan(args.block_elems, 4096, args.threads))
+    plan = en.plan()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    b, fixed = P["b"], P["fixed"]
+    sst = solvers.solver_stream(dev)
+    hvp_launches = 2 if plan.sizes["n_shared"] > 0 else 1
+
+    # ---- the dominant kernel: FP32 HVP (roofline), and the FP64 HVP
+    g = torch.Generator(device=dev).manual_seed(1234 + rank)
+    v = torch.randn(ndof, dtype=torch.float32, device=dev, generator=g)
+    y = torch.empty_like(v)
+    hvp_ms, _ = _hvp_timing(en, v, y, flush, max(args.steps, 20), args.warmup, dev)
+    v64, y64 = v.double(), torch.empty(ndof, dtype=torch.float64, device=dev)
+    hvp64_ms, _ = _hvp_timing(en, v64, y64, flush, 5, 2, dev)
+
+    def mixed():
+        return solvers.mixed_cg(en, b, fixed=fixed, rtol=RTOL, inner_rtol=args.inner_rtol,
+                                max_inner=args.max_iter, check_every=args.check_every,
+                                raise_on_fail=False)
+
+    # ---- headline: mixed-precision solves, device-timed on the solver's stream
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        r = mixed()
+    torch.cuda.synchronize()
+    replicas.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    results = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            evs[i][0].record(sst)
+            results.append(mixed())
+            evs[i][1].record(sst)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    clocks["window"] = "nvidia-smi every 200 ms over the timed solves"
+    ms = [a.elapsed_time(bb) for a, bb in evs]
+    replicas.barrier()
+    ms_step = replicas.max_over_ranks(float(np.mean(ms)))
+    value = replicas.sum_over_ranks(1.0) / (ms_step * 1e-3)
+    conv = all(rr.converged and rr.rel_res <= RTOL for rr in results)
+    inner = results[-1].iterations
+    outer = results[-1].outer
+    # launches per mixed solve: per inner iteration the HVP plus 3 CG kernels; per
+    # refinement the FP64 HVP, 3 residual/norm kernels, the scale-down and the CG restart
+    # (HVP + 4 kernels) and the update; 3 set-up kernels, and the Jacobi diagonal
+    launches_per_solve = (inner * (hvp_launches + 3) + (outer + 1) * (hvp_launches + 3)
+                          + outer * (hvp_launches + 6) + 3 + hvp_launches)
+
+    # ---- e2e through the public API: b from pinned host memory, x back to the host
+    bh = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
+    bh.copy_(b.cpu())
+    xh = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
+    cur = torch.cuda.current_stream(dev)
+
+    def e2e_step():
+        bd = bh.to(dev, non_blocking=True)
+        rr = solvers.mixed_cg(en, bd, fixed=fixed, rtol=RTOL, inner_rtol=args.inner_rtol,
+                              max_inner=args.max_iter, check_every=args.check_every,
+                              raise_on_fail=False)
+        xh.copy_(rr.x, non_blocking=True)
+        return rr
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 5))
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(cur)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e.record(cur)
+    torch.cuda.synchronize()
+    e2e_ms = replicas.max_over_ranks(s.elapsed_time(e) / e2e_steps)
+    e2e_value = replicas.sum_over_ranks(1.0) / (e2e_ms * 1e-3)
+
+    # ---- the plain FP64 solve (the reference user's algorithm) on the GPU
+    fp64 = None
+    if args.fp64_solves:
+        solvers.cg(en, b, fixed=fixed, rtol=RTOL, maxiter=args.max_iter,
+                   check_every=args.check_every, raise_on_fail=False)
+        ts = []
+        for _ in range(args.fp64_solves):
+            flush.fill_(2.0)
+            s.record(sst)
+            r64 = solvers.cg(en, b, fixed=fixed, rtol=RTOL, maxiter=args.max_iter,
+                             check_every=args.check_every, raise_on_fail=False)
+            e.record(sst)
+            torch.cuda.synchronize()
+            ts.append(s.elapsed_time(e))
+        fp64 = {"ms_per_solve": float(np.mean(ts)), "solves_per_s": 1e3 / float(np.mean(ts)),
+                "iterations": r64.iterations, "rel_res": r64.rel_res,
+                "converged": r64.converged, "dtype": "f64",
+                "mixed_speedup": float(np.mean(ts)) / ms_step}
+
+    # ---- roofline of the HVP
+    nn, ne = P["n_nodes"], P["n_elems"]
+    alg_bytes = 2 * 4 * ndof + 4 * 8 * ne + 4 * 3 * nn
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / (hvp_ms * 1e-3) / 1e9
+    traffic = _profile_value(TRAFFIC_PROFILE, "traffic_bytes_per_hvp_128") if n == N_CELLS else None
+    replicas.barrier()
+    if rank != 0:
+        return
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        its = fp64["iterations"] if fp64 else FP64_CG_ITERATIONS.get(n, 1000)
+        cores = os.cpu_count() or 1
+        cb = CpuBrickCg(n, cores)
+        sec = cb.time_iterations(1, args.cpu_iterations)
+        cb.close()
+        cpu = {"value": 1.0 / (sec * its), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"numpy restatement of FP64 Jacobi-CG on the same {n}^3 system: "
+                         f"{args.cpu_iterations} iterations (HVP over {cores} processes) at "
+                         f"{sec:.3f} s each, x {its} iterations (the FP64 solver's count)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "precision": "FP32 HVP and inner CG vectors; FP64 true residual, refinement update "
+                     "and every dot product; each solve stops at FP64 rel-res <= 1e-10",
+        "data": "synthetic", "config": workload_config(n),
+        "l2": "flushed before every solve (256 MiB write); solve working set > L2",
+        "converged": conv, "rel_res": results[-1].rel_res, "inner_iterations": inner,
+        "refinements": outer,
+        "gpu_launches": args.steps * launches_per_solve,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ndof * 8,
+                "d2h_bytes_per_step": ndof * 8, "ms_per_step": e2e_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": "FP32 HVP",
+                     "ms": hvp_ms, "peak_source": peak_kind, "algorithmic_bytes": alg_bytes},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "fp64_solve": fp64,
+        "hvp": {"f32_ms": hvp_ms, "f32_gdof_s": ndof / (hvp_ms * 1e-3) / 1e9,
+                "f64_ms": hvp64_ms, "f64_gdof_s": ndof / (hvp64_ms * 1e-3) / 1e9,
+                "launches_per_hvp": hvp_launches},
+        "plan": {k: plan.stats()[k] for k in ("block_elems", "threads", "n_blocks",
+                                              "shared_fraction", "n_lattice_blocks")},
+        "wall_s_timed_region": wall,
+    }
+    if tune:
+        line["autotune"] = tune
+    if args.batched:
+        line["batched"] = bench_batched(dev, args)
+    if args.serving:
+        line["serving"] = bench_serving(dev, args)
+    if args.newton:
+        line["newton"] = bench_newton(dev, args)
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- extras
+BATCH_TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "batch_solve_poisson_4096.md")
 
 
 def bench_batched(dev, args):
@@ -275,12 +594,19 @@ def bench_batched(dev, args):
            "max_inner_iterations": int(r.iterations.max()),
            "mean_refinements": float(r.refinements.mean()),
            "threads": sysm.threads, "ctas_per_sm": sysm.ctas_per_sm, "autotune": tune,
-           "gpu_launches_per_batch": 1,
-           "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": alg / t / 1e9 / peak, "peak_source": kind,
-                        "algorithmic_bytes": alg,
-                        "note": "inner-iteration bytes (6 B per ELL entry + 36 B of vector "
-                                "traffic per row); systems in flight are largely L2-resident"}}
+           "gpu_launches_per_batch": 1}
+    # DRAM bytes of one batched launch (ncu, committed summary) over the measured time:
+    # the HBM fraction.  The inner-iteration byte count is mostly served by the L2
+    # (systems in flight fit in it) and is reported separately as an L2-inclusive rate.
+    dram = _profile_value(BATCH_TRAFFIC_PROFILE, f"dram_bytes_per_batch_{len(meshes)}")
+    rf = {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": kind,
+          "l2_inclusive_gbs": alg / t / 1e9, "l2_inclusive_bytes": alg,
+          "note": "achieved = DRAM bytes of one launch (ncu) / measured time; "
+                  "l2_inclusive counts 6 B per ELL entry + 36 B of vector traffic per row "
+                  "and inner iteration, most of it served by the L2"}
+    if dram:
+        rf.update(achieved=dram / t / 1e9, frac=dram / t / 1e9 / peak, traffic=dram)
+    out["roofline"] = rf
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = _cpu_batched_sample(meshes, kappas, args.cpu_seconds)
     return out
@@ -363,7 +689,6 @@ def _cpu_serving_sample():
         y = omat.hvp(op, law, None, zz)
         return np.where(fixed, z, y)
 
-    diag = np.ones_like(b)
     cols = np.zeros_like(b)
     ndof = b.size
     # Jacobi diagonal from unit probes of the element tangents
@@ -471,229 +796,82 @@ def _cpu_newton_sample(n=10):
                       f"iterations, numpy element tangents + scipy sparse direct solve, {dt:.1f} s"}
 
 
-def run_ours(args):
+# ----------------------------------------------------------------------------- drivers
+def run_driver(args):
+    """Workload drivers that the ncu summaries under profiles/ were captured on:
+
+    * ``brick`` / ``kuhn`` / ``kuhn-le``: ``--repeats`` fused HVPs (``--prec``) of the
+      clamped brick (``--size`` cells per side), the Neo-Hookean Kuhn block, or the same
+      Kuhn mesh with the linear-elastic law;
+    * ``brick-cg``: ``--repeats`` Jacobi-CG iterations on the clamped brick;
+    * ``batch``: the seeded random unit-square batch of ``--batched`` meshes, solved
+      ``--repeats`` times."""
     import torch
 
-    from tatva_gb300 import _lib, autotune, solvers
-    from tatva_gb300._device import ptr
+    from tatva_gb300 import _lib, solvers
+    from tatva_gb300.materials import LinearElastic
+    from tatva_gb300.problems import clamped_brick, stretched_kuhn
 
-    from tatva_gb300 import replicas
+    dtype = torch.float64 if args.prec == "f64" else torch.float32
+    name, n, reps = args.driver, args.size, args.repeats
+    if name == "batch":
+        from tatva_gb300 import batched
 
-    ws, rank, local = replicas.world()
-    torch.cuda.set_device(local)
-    replicas.init("nccl")
-    dev = torch.device("cuda", local)
-    P = brick_problem(args.size, dev)
-    en = P["energy"]
-    ndof = en.n_dofs
-    tune = autotune.tune(en, dtype=torch.float32) if args.autotune else None
-    if not args.autotune and args.block_elems:
-        en.use_plan(P["op"].plan(args.block_elems, 4096, args.threads))
-    plan = en.plan()
-    g = torch.Generator(device=dev).manual_seed(1234 + rank)
-    v = torch.randn(ndof, dtype=torch.float32, device=dev, generator=g)
-    y = torch.empty_like(v)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    st = torch.cuda.current_stream()
-
-    def hvp_step(vv, out):
-        en.apply(_lib.TG_MODE_HVP, None, vv, out=out)
-
-    # the HVP is captured once in a CUDA graph and replayed each step, so that host-side
-    # launch latency of the Python wrapper does not leak into the device time
-    side = torch.cuda.Stream(device=dev)
-    side.wait_stream(st)
-    with torch.cuda.stream(side):
-        hvp_step(v, y)
-    st.wait_stream(side)
-    torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph):
-        hvp_step(v, y)
-    for _ in range(args.warmup):
-        flush.fill_(1.0)
-        graph.replay()
-    torch.cuda.synchronize()
-    replicas.barrier()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
+        meshes, kappas, _ = batched.random_unit_squares(args.batched, seed=0)
+        systems, b, info = batched.poisson_batch(meshes, kappas, device="cuda")
+        res = None
+        for _ in range(reps):
+            res = systems.solve(b)
+        print(dict(info, converged=res.converged, max_rel_res=float(res.rel_res.max()),
+                   seconds=res.seconds))
+        return
+    if name == "brick-cg":
+        P = clamped_brick(n, "cuda")
+        bb = P["b"].to(dtype)
+        solvers.cg(P["energy"], bb, fixed=P["fixed"], dtype=dtype, rtol=1e-30, maxiter=reps,
+                   check_every=min(reps, 50), raise_on_fail=False)  # warm-up, graph build
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for i in range(args.steps):
-            flush.fill_(float(i))
-            evs[i][0].record(st)
-            graph.replay()
-            evs[i][1].record(st)
+        r = solvers.cg(P["energy"], bb, fixed=P["fixed"], dtype=dtype, rtol=1e-30,
+                       maxiter=reps, check_every=min(reps, 50), raise_on_fail=False)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        # the timed region is shorter than the sampling period: keep the same work
-        # running (untimed) for about a second so the sampler sees the GPU under it
-        t1 = time.perf_counter()
-        while time.perf_counter() - t1 < 1.0:
-            for _ in range(50):
-                flush.fill_(0.5)
-                graph.replay()
-            torch.cuda.synchronize()
-    clocks = clk.summary()
-    clocks["window"] = ("nvidia-smi every 200 ms over the timed steps plus ~1 s of the same "
-                        "flush + HVP steps run untimed right after them")
-    ms = [a.elapsed_time(b) for a, b in evs]
-    replicas.barrier()
-    ms_step = replicas.max_over_ranks(float(np.mean(ms)))
-    value = replicas.sum_over_ranks(ndof) / (ms_step * 1e-3) / 1e9
-
-    # ---- e2e through the public API with host buffers
-    vh = torch.empty(ndof, dtype=torch.float32, pin_memory=True)
-    vh.copy_(v.cpu())
-    yh = torch.empty(ndof, dtype=torch.float32, pin_memory=True)
-    for _ in range(max(1, args.warmup)):
-        yh.copy_(en.hvp(None, vh.to(dev, non_blocking=True)), non_blocking=True)
-    torch.cuda.synchronize()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record(st)
-    for _ in range(args.steps):
-        yh.copy_(en.hvp(None, vh.to(dev, non_blocking=True)), non_blocking=True)
-    e.record(st)
-    torch.cuda.synchronize()
-    e2e_seq_ms = replicas.max_over_ranks(s.elapsed_time(e) / args.steps)
-
-    # the same loop pipelined as a serving loop runs it: input copy, HVP and result
-    # copy on three streams with double buffers, so that step i's result copy and step
-    # i+1's input copy overlap step i's HVP; every step still moves its input in and
-    # its result out
-    s_in, s_cmp, s_out = (torch.cuda.Stream(device=dev) for _ in range(3))
-    dvs = [torch.empty(ndof, dtype=torch.float32, device=dev) for _ in range(2)]
-    dys = [torch.empty(ndof, dtype=torch.float32, device=dev) for _ in range(2)]
-    yhs = [torch.empty(ndof, dtype=torch.float32, pin_memory=True) for _ in range(2)]
-    ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("in", "cmp", "out")}
-
-    def pipelined(n_steps, start=None):
-        for i in range(n_steps):
-            b = i % 2
-            if i >= 2:
-                s_in.wait_event(ev["cmp"][b])   # dvs[b] no longer read
-                s_cmp.wait_event(ev["out"][b])  # dys[b] already copied out
-            if i == 0 and start is not None:
-                start.record(s_in)
-            with torch.cuda.stream(s_in):
-                dvs[b].copy_(vh, non_blocking=True)
-                ev["in"][b].record(s_in)
-            s_cmp.wait_event(ev["in"][b])
-            with torch.cuda.stream(s_cmp):
-                en.apply(_lib.TG_MODE_HVP, None, dvs[b], out=dys[b])
-                ev["cmp"][b].record(s_cmp)
-            s_out.wait_event(ev["cmp"][b])
-            with torch.cuda.stream(s_out):
-                yhs[b].copy_(dys[b], non_blocking=True)
-                ev["out"][b].record(s_out)
-
-    torch.cuda.synchronize()
-    pipelined(max(2, args.warmup))
-    torch.cuda.synchronize()
-    s = torch.cuda.Event(enable_timing=True)
-    e = torch.cuda.Event(enable_timing=True)
-    pipelined(args.steps, start=s)
-    e.record(s_out)
-    torch.cuda.synchronize()
-    e2e_ms = replicas.max_over_ranks(s.elapsed_time(e) / args.steps)
-    e2e_value = replicas.sum_over_ranks(ndof) / (e2e_ms * 1e-3) / 1e9
-
-    # ---- roofline of the HVP
-    nn, ne = P["n_nodes"], P["n_elems"]
-    alg_bytes = 2 * 4 * ndof + 4 * 8 * ne + 4 * 3 * nn
-    peak, peak_kind = _peaks()
-    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
-    traffic = _traffic_from_profile() if args.size == N_CELLS else None
-
-    # ---- FP64 HVP and the solves (rank 0 only reports)
-    y64 = torch.empty(ndof, dtype=torch.float64, device=dev)
-    v64 = v.double()
-    for _ in range(2):
-        en.apply(_lib.TG_MODE_HVP, None, v64, out=y64)
-    s.record(st)
-    for _ in range(5):
-        en.apply(_lib.TG_MODE_HVP, None, v64, out=y64)
-    e.record(st)
-    torch.cuda.synchronize()
-    ms64 = s.elapsed_time(e) / 5
-    solve = None
-    if args.solve:
-        b, fixed = P["b"], P["fixed"]
-        r64 = solvers.cg(en, b, fixed=fixed, rtol=1e-10, maxiter=args.max_iter,
-                         check_every=100, raise_on_fail=False)
-        rmx = solvers.mixed_cg(en, b, fixed=fixed, rtol=1e-10, inner_rtol=args.inner_rtol,
-                               max_inner=args.max_iter, check_every=100, raise_on_fail=False)
-        solve = {
-            "rtol": 1e-10,
-            "fp64": {"seconds": r64.seconds, "iterations": r64.iterations,
-                     "rel_res": r64.rel_res, "converged": r64.converged, "message": r64.message,
-                     "solves_per_s": 1.0 / r64.seconds},
-            "mixed": {"seconds": rmx.seconds, "inner_iterations": rmx.iterations,
-                      "refinements": rmx.outer, "rel_res": rmx.rel_res,
-                      "converged": rmx.converged, "message": rmx.message, "solves_per_s": 1.0 / rmx.seconds},
-            "speedup_mixed_vs_fp64": r64.seconds / rmx.seconds,
-        }
-    replicas.barrier()
-    if rank != 0:
+        dt = time.perf_counter() - t0
+        print(name, n, P["energy"].n_dofs, r.iterations,
+              f"{1e6 * dt / max(r.iterations, 1):.1f} us/it")
         return
-    cpu = None
-    if not args.no_cpu_baseline:
-        cb = CpuHvp(32, processes=1)
-        gc, dtc, reps = cb.measure(args.cpu_seconds)
-        ndc = cb.ndof
-        cpu = {"value": gc, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"numpy restatement (FP64) of the HVP on a 32^3 brick ({ndc} dofs), "
-                         f"{reps} repetitions, {dtc * 1e3:.1f} ms each"}
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"hex8 linear-elastic HVP, structured brick {args.size}^3 "
-                               f"({ne} elements, {ndof} dofs), E=1 nu=0.3, 2x2x2 Gauss",
-                   "l2": "flushed before every step (256 MiB write)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "plan": {k: plan.stats()[k] for k in ("block_elems", "threads", "n_blocks",
-                                                          "shared_fraction")}},
-        "gpu_launches": args.steps * (2 if plan.sizes["n_shared"] > 0 else 1),
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ndof * 4,
-                "d2h_bytes_per_step": ndof * 4, "ms_per_step": e2e_ms,
-                "pipeline": "input copy / HVP / result copy on three streams, double buffers",
-                "sequential_ms_per_step": e2e_seq_ms},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": peak_kind, "algorithmic_bytes": alg_bytes},
-        "clocks": clocks,
-        "cpu_baseline": cpu,
-        "fp64_hvp": {"ms": ms64, "gdof_s": ndof / (ms64 * 1e-3) / 1e9},
-        "solve": solve,
-        "wall_s_timed_region": wall,
-    }
-    if tune:
-        line["autotune"] = tune
-    if args.batched:
-        line["batched"] = bench_batched(dev, args)
-    if args.serving:
-        line["serving"] = bench_serving(dev, args)
-    if args.newton:
-        line["newton"] = bench_newton(dev, args)
-    print(json.dumps(line), flush=True)
+    if name == "brick":
+        P = clamped_brick(n, "cuda")
+        en, u = P["energy"], None
+    elif name in ("kuhn", "kuhn-le"):
+        P = stretched_kuhn(n, "cuda")
+        en = P["energy"] if name == "kuhn" else LinearElastic(P["op"], 1.0, 1.0)
+        u = None if name != "kuhn" else torch.zeros(en.n_dofs, dtype=dtype, device="cuda")
+    else:
+        raise SystemExit(f"unknown driver {name}")
+    v = torch.ones(en.n_dofs, dtype=dtype, device="cuda")
+    y = torch.empty_like(v)
+    for _ in range(reps):
+        en.apply(_lib.TG_MODE_HVP, u, v, out=y)
+    torch.cuda.synchronize()
+    print(name, n, en.n_dofs, float(y.abs().sum()))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10, help="timed solves")
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_CELLS)
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--block-elems", type=int, default=0, help="plan when --autotune 0")
     ap.add_argument("--threads", type=int, default=256, help="plan when --autotune 0")
-    ap.add_argument("--solve", type=int, default=1)
     ap.add_argument("--max-iter", type=int, default=20000)
     ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--check-every", type=int, default=50)
+    ap.add_argument("--fp64-solves", type=int, default=2, help="timed FP64 solves (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-iterations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched", type=int, default=4096, help="meshes in the batched solve (0: skip)")
     ap.add_argument("--serving", type=int, default=200, help="requests in the serving run (0: skip)")
@@ -701,7 +879,13 @@ def main():
     ap.add_argument("--newton", type=int, default=96, help="Kuhn cells per side (0: skip)")
     ap.add_argument("--newton-steps", type=int, default=10)
     ap.add_argument("--hbm-budget", type=int, default=32, help="serving HBM budget, GiB")
+    ap.add_argument("--driver", default="", help="run a profiling workload driver instead")
+    ap.add_argument("--repeats", type=int, default=3, help="driver repetitions")
+    ap.add_argument("--prec", default="f32", choices=["f32", "f64"], help="driver precision")
     args = ap.parse_args()
+    if args.driver:
+        run_driver(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -227,8 +227,9 @@ TG_API int tg_apply(int elem, int prec, int mode, const tg_material* mat, const 
  * fixed array of TG_NOALLOC_SCRATCH_BYTES per device inside the library; plans whose
  * tg_apply_workspace_bytes exceed it are rejected with TG_ERR_WORKSPACE.  Nothing in
  * the array needs to start at zero (each slot is written before it is read).  The
- * first call on a device looks the array's address up and caches it: make that call
- * before any stream capture.  Calls that overlap on the GPU share the array and
+ * first call in a CUDA context looks the array's address up and caches it under the
+ * context's id (a device reset gives a new context and a fresh lookup): make that
+ * call before any stream capture.  Calls that overlap on the GPU share the array and
  * race; calls ordered on one stream are safe.  Allocates nothing.              */
 #define TG_NOALLOC_SCRATCH_BYTES (8u << 20)
 TG_API int tg_apply_noalloc(int elem, int prec, int mode, const tg_material* mat,
@@ -339,7 +340,9 @@ TG_API int tg_spmv_blocks3(int prec, int64_t n_rows, const int32_t* indptr,
 TG_API int tg_csr_diagonal(int prec, int64_t n_rows, const int32_t* indptr, const int32_t* indices,
                     const void* data, void* diag, void* stream);
 /* out_dev[0] = sum x_i y_i accumulated in FP64, deterministic (fixed partition
- * and tree order independent of the GPU).  out_dev is a device double.        */
+ * and tree order independent of the GPU).  out_dev is a device double.  x and y
+ * are read with 16-byte vector loads: both must be 16-byte aligned, else
+ * TG_ERR_VALUE (a slice at an odd element offset must be copied first).      */
 TG_API size_t tg_dot_workspace_bytes(void);
 TG_API int tg_dot(int prec, const void* x, const void* y, int64_t n, double* out_dev,
            void* workspace, size_t workspace_bytes, void* stream);
@@ -393,7 +396,8 @@ TG_API int tg_operator_apply(const tg_operator_desc* op, const void* x, void* y,
 /* Jacobi-preconditioned CG, all vectors of precision op->prec, scalars and dot
  * products in FP64 on the device.  Solves A x = b from the given x.  The loop runs
  * `check_every` iterations per CUDA graph replay between host convergence checks
- * and never exceeds max_iter.                                                  */
+ * and never exceeds max_iter.  b and x must be 16-byte aligned (vector loads and
+ * stores), else TG_ERR_VALUE.                                                  */
 TG_API size_t tg_cg_workspace_bytes(const tg_operator_desc* op);
 TG_API int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, const void* diag,
                 double rtol, int max_iter, int check_every, void* workspace,
@@ -401,7 +405,8 @@ TG_API int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, const
 
 /* Mixed precision: FP32 Jacobi-CG inner solves on op32 (FP32 HVP, FP64 dots),
  * FP64 iterative refinement with the true residual r = b - A64 x on op64.
- * b, x, diag64 are FP64; converges to ||b - A64 x|| <= rtol ||b||.           */
+ * b, x, diag64 are FP64; converges to ||b - A64 x|| <= rtol ||b||.  b must be
+ * 16-byte aligned (vector loads), else TG_ERR_VALUE.                          */
 TG_API size_t tg_mixed_workspace_bytes(const tg_operator_desc* op64, const tg_operator_desc* op32);
 TG_API int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_desc* op32,
                    const double* b, double* x, const double* diag64, double rtol,

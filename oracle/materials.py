@@ -183,12 +183,12 @@ def residual(op: OracleOperator, law, u):
 def hvp(op: OracleOperator, law, u, v):
     """jax.jvp(jax.grad(E), (u,), (v,))[1] in closed form."""
     nv = law.n_values
-    if u is None:  # linear laws: the HVP does not depend on u
-        u = np.zeros_like(np.asarray(v, dtype=np.float64))
-    U = _as_nodal(op, u, nv)
     V = _as_nodal(op, v, nv)
-    H = op.grad(U)
     dH = op.grad(V)
+    if u is None:  # linear laws: the HVP does not depend on u (linearised at u = 0)
+        H = np.zeros(dH.shape)
+    else:
+        H = op.grad(_as_nodal(op, u, nv))
     dP = law.dflux(H, dH)
     w = op.get_integration_weights()
     return op.grad_transpose(dP * w[:, :, None, None]).reshape(-1)

@@ -29,13 +29,16 @@ class OracleOperator:
         return self.elements.shape[0]
 
     def geometry(self):
-        """Per (e,q): dNdX (E,Q,d,n) and detJ (E,Q).  element/base.py:90-115."""
-        X = self.coords[self.elements]  # (E, n, d)
-        J = np.einsum("qdn,enk->eqdk", self.dN, X)
-        detJ = np.linalg.det(J)
-        Jinv = np.linalg.inv(J)
-        dNdX = np.einsum("eqkd,qdn->eqkn", Jinv, self.dN)
-        return dNdX, detJ
+        """Per (e,q): dNdX (E,Q,d,n) and detJ (E,Q).  element/base.py:90-115.
+        Computed once per operator (coordinates and connectivity are fixed)."""
+        if getattr(self, "_geometry", None) is None:
+            X = self.coords[self.elements]  # (E, n, d)
+            J = np.einsum("qdn,enk->eqdk", self.dN, X)
+            detJ = np.linalg.det(J)
+            Jinv = np.linalg.inv(J)
+            dNdX = np.einsum("eqkd,qdn->eqkn", Jinv, self.dN)
+            self._geometry = (dNdX, detJ)
+        return self._geometry
 
     def get_integration_weights(self):
         _, detJ = self.geometry()
@@ -100,16 +103,28 @@ class OracleOperator:
         n_nodes = n_nodes or self.coords.shape[0]
         dNdX, _ = self.geometry()
         contrib = np.einsum("eqdn,eq...d->en...", dNdX, flux)
-        out = np.zeros((n_nodes,) + contrib.shape[2:], dtype=contrib.dtype)
-        np.add.at(out, self.elements, contrib)
-        return out
+        return _scatter_add(self.elements, contrib, n_nodes)
 
     def eval_transpose(self, quad_values, n_nodes=None):
         n_nodes = n_nodes or self.coords.shape[0]
         contrib = np.einsum("qn,eq...->en...", self.N, quad_values)
-        out = np.zeros((n_nodes,) + contrib.shape[2:], dtype=contrib.dtype)
-        np.add.at(out, self.elements, contrib)
-        return out
+        return _scatter_add(self.elements, contrib, n_nodes)
+
+
+def _scatter_add(elements, contrib, n_nodes):
+    """out[elements[e, a]] += contrib[e, a, ...], the adds in (e, a) order (the order of
+    np.add.at, done per trailing component with np.bincount, which is much faster)."""
+    idx = np.asarray(elements).reshape(-1)
+    flat = contrib.reshape(idx.size, -1)
+    out = np.zeros((n_nodes, flat.shape[1]), dtype=contrib.dtype)
+    for c in range(flat.shape[1]):
+        col = flat[:, c]
+        if np.iscomplexobj(col):
+            out[:, c] = (np.bincount(idx, weights=col.real, minlength=n_nodes)
+                         + 1j * np.bincount(idx, weights=col.imag, minlength=n_nodes))
+        else:
+            out[:, c] = np.bincount(idx, weights=col, minlength=n_nodes)
+    return out.reshape((n_nodes,) + contrib.shape[2:])
 
 
 def project(op: OracleOperator, field, fixed_nodes=None, fixed_values=None):

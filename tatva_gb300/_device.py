@@ -37,6 +37,12 @@ def ptr(t: torch.Tensor | None) -> int | None:
     return t.data_ptr()
 
 
+def aligned16(t: torch.Tensor) -> torch.Tensor:
+    """``t`` itself when its data starts on a 16-byte boundary, else a fresh copy (the
+    solver and dot kernels read vectors four entries at a time)."""
+    return t if t.data_ptr() % 16 == 0 else t.clone()
+
+
 def stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 

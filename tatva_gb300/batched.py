@@ -240,24 +240,3 @@ def poisson_batch(meshes, kappas=None, f: float = 1.0, fixed=None, device=None):
 
 __all__ = ["BatchResult", "BatchedSystems", "boundary_nodes_tri3", "concat_meshes",
            "poisson_batch", "random_unit_squares"]
-
-
-def _main(argv=None) -> None:
-    """``python -m tatva_gb300.batched [n_meshes] [repeats]``: build the seeded random
-    unit-square batch and solve it ``repeats`` times (a workload driver for profiling)."""
-    import sys
-
-    args = list(sys.argv[1:] if argv is None else argv)
-    count = int(args[0]) if args else 512
-    repeats = int(args[1]) if len(args) > 1 else 2
-    meshes, kappas, _ = random_unit_squares(count, seed=0)
-    systems, b, info = poisson_batch(meshes, kappas, device="cuda")
-    res = None
-    for _ in range(repeats):
-        res = systems.solve(b)
-    print(dict(info, converged=res.converged, max_rel_res=float(res.rel_res.max()),
-               seconds=res.seconds))
-
-
-if __name__ == "__main__":
-    _main()

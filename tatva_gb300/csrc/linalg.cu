@@ -593,12 +593,25 @@ extern "C" int tg_csr_apply_dirichlet(int prec, int64_t n_rows, const int32_t* i
   });
 }
 
+// The vector kernels read and write four entries at a time (16-byte loads and
+// stores); a caller's pointer at an odd offset would fault, so it is refused here.
+static int check_align16(const void* p, const char* fn, const char* what) {
+  if (reinterpret_cast<uintptr_t>(p) % 16 != 0)
+    return set_error(TG_ERR_VALUE,
+                     "%s: %s must be 16-byte aligned (address %p); copy the vector into a "
+                     "fresh buffer first",
+                     fn, what, p);
+  return TG_OK;
+}
+
 extern "C" size_t tg_dot_workspace_bytes(void) { return (size_t)DOT_CHUNKS * 2 * sizeof(double); }
 
 extern "C" int tg_dot(int prec, const void* x, const void* y, int64_t n, double* out_dev,
                       void* workspace, size_t workspace_bytes, void* stream) {
   if (n < 0) return set_error(TG_ERR_VALUE, "negative size");
   TG_TRY(check_ptr(out_dev, "out"));
+  TG_TRY(check_align16(x, "tg_dot", "x"));
+  TG_TRY(check_align16(y, "tg_dot", "y"));
   if (workspace_bytes < tg_dot_workspace_bytes())
     return set_error(TG_ERR_WORKSPACE, "tg_dot: workspace too small");
   cudaStream_t st = as_stream(stream);
@@ -815,6 +828,8 @@ extern "C" int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, c
   TG_TRY(check_ptr(b, "b"));
   TG_TRY(check_ptr(x, "x"));
   TG_TRY(check_ptr(diag, "diag"));
+  TG_TRY(check_align16(b, "tg_cg_solve", "b"));
+  TG_TRY(check_align16(x, "tg_cg_solve", "x"));
   if (workspace_bytes < cg_bytes(op)) return set_error(TG_ERR_WORKSPACE, "tg_cg_solve: workspace too small");
   if (!(rtol > 0.0) || max_iter < 0) return set_error(TG_ERR_VALUE, "bad rtol / max_iter");
   cudaStream_t st = as_stream(stream);
@@ -851,7 +866,7 @@ extern "C" size_t tg_mixed_workspace_bytes(const tg_operator_desc* op64,
   if (!op64 || !op32) return 0;
   const int64_t n = op_ndofs(op64);
   return cg_bytes(op32) + align256(tg_operator_workspace_bytes(op64)) +
-         2 * align256((size_t)n * sizeof(double)) + 3 * align256((size_t)n * sizeof(float)) +
+         align256((size_t)n * sizeof(double)) + 3 * align256((size_t)n * sizeof(float)) +
          align256(DOT_CHUNKS * sizeof(double)) + align256(8 * sizeof(double));
 }
 
@@ -865,6 +880,7 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
   TG_TRY(check_ptr(b, "b"));
   TG_TRY(check_ptr(x, "x"));
   TG_TRY(check_ptr(diag64, "diag64"));
+  TG_TRY(check_align16(b, "tg_mixed_solve", "b"));
   if (op64->prec != TG_F64 || op32->prec != TG_F32)
     return set_error(TG_ERR_TYPE, "tg_mixed_solve: op64 must be FP64 and op32 FP32");
   const int64_t n = op_ndofs(op64);
@@ -877,7 +893,6 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
   const size_t ab64 = tg_operator_workspace_bytes(op64);
   void* aws64 = c.take(ab64);
   double* r64 = (double*)c.take(n * sizeof(double));
-  double* t64 = (double*)c.take(n * sizeof(double));
   float* r32 = (float*)c.take(n * sizeof(float));
   float* d32 = (float*)c.take(n * sizeof(float));
   float* diag32 = (float*)c.take(n * sizeof(float));
@@ -919,7 +934,6 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
     TG_TRY(launch_check("mixed: update"));
     ++outer;
   }
-  (void)t64;
   if (stats) {
     stats->status = rc;
     stats->iterations = total_inner;

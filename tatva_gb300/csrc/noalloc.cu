@@ -19,10 +19,17 @@
 // them) race on it and give wrong results.  Calls issued on one stream are ordered and
 // safe.
 //
-// First call on a device: the array's device address is looked up with
-// cudaGetSymbolAddress, with that device current, and cached per device.  That lookup
-// (and the lazy load of the library's device code it can trigger) is set-up work, so
-// make the first call on each device before any stream capture begins.
+// First call in a CUDA context: the array's device address is looked up with
+// cudaGetSymbolAddress, with that context's device current, and cached under the
+// context's id (cuCtxGetId, reached through cudaGetDriverEntryPointByVersion, so the
+// library needs no link to the driver library).  A device reset, or another context
+// made current on the same device, has a new id: the next call looks the address up
+// again instead of using one from a module that no longer exists.  That lookup (and
+// the lazy load of the library's device code it can trigger) is set-up work, so make
+// the first call on each device, and the first after a reset, before any stream
+// capture begins.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "tg_common.cuh"
@@ -35,25 +42,67 @@ constexpr int kMaxDevices = 64;
 // 8 MiB of partial slots: 2M FP32 or 1M FP64 values.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[TG_NOALLOC_SCRATCH_BYTES];
 
-std::mutex g_setup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-// Returns the scratch address on the current device, looking it up on first use.
+std::mutex g_setup_mutex;
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+struct Cached {
+  unsigned long long ctx_id;
+  void* ptr;
+};
+Cached g_scratch[kMaxDevices] = {};
+
+// Id of the context current on the calling thread (the primary context of `dev` after
+// cudaGetDevice has made sure one exists).  Called with g_setup_mutex held.
+int current_context_id(unsigned long long* id) {
+  if (!g_ctx_current || !g_ctx_id) {
+    void* f0 = nullptr;
+    void* f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0, q1;
+    TG_TRY(cuda_check(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000,
+                                                       cudaEnableDefault, &q0),
+                      "tg_apply_noalloc: driver entry point cuCtxGetCurrent"));
+    TG_TRY(cuda_check(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000,
+                                                       cudaEnableDefault, &q1),
+                      "tg_apply_noalloc: driver entry point cuCtxGetId"));
+    if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+      return set_error(TG_ERR_UNSUPPORTED,
+                       "tg_apply_noalloc: the driver does not provide cuCtxGetCurrent / cuCtxGetId");
+    g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+    g_ctx_id = reinterpret_cast<CtxGetIdFn>(f1);
+  }
+  CUcontext ctx = nullptr;
+  if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx)
+    return set_error(TG_ERR_CUDA, "tg_apply_noalloc: no current CUDA context");
+  if (g_ctx_id(ctx, id) != CUDA_SUCCESS)
+    return set_error(TG_ERR_CUDA, "tg_apply_noalloc: cuCtxGetId failed");
+  return TG_OK;
+}
+
+// Returns the scratch address in the current context, looking it up on first use in
+// that context.
 int scratch_on_current_device(void** out) {
   int dev = -1;
   TG_TRY(cuda_check(cudaGetDevice(&dev), "tg_apply_noalloc: cudaGetDevice"));
   if (dev < 0 || dev >= kMaxDevices)
     return set_error(TG_ERR_UNSUPPORTED, "tg_apply_noalloc: device ordinal %d >= %d", dev,
                      kMaxDevices);
+  // re-selecting the current device makes its primary context current (CUDA >= 12
+  // initialises it here) so that the context query below has one to name
+  TG_TRY(cuda_check(cudaSetDevice(dev), "tg_apply_noalloc: cudaSetDevice"));
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
+  unsigned long long id = 0;
+  TG_TRY(current_context_id(&id));
+  if (!g_scratch[dev].ptr || g_scratch[dev].ctx_id != id) {
     void* p = nullptr;
     TG_TRY(cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch),
                       "tg_apply_noalloc: cudaGetSymbolAddress of the scratch array"));
     if (!p) return set_error(TG_ERR_CUDA, "tg_apply_noalloc: scratch array has no address");
-    g_scratch_ptr[dev] = p;
+    g_scratch[dev] = Cached{id, p};
   }
-  *out = g_scratch_ptr[dev];
+  *out = g_scratch[dev].ptr;
   return TG_OK;
 }
 

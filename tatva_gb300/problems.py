@@ -72,55 +72,3 @@ def stretched_kuhn(n: int, device, jitter: float = 0.2, seed: int = 0, mu: float
 
 
 __all__ = ["clamped_brick", "stretched_kuhn"]
-
-
-def _main(argv=None) -> None:
-    """``python -m tatva_gb300.problems {brick,kuhn,kuhn-le} N [repeats] [f32|f64]``: run
-    the fused HVP of a benchmark problem ``repeats`` times; ``brick-cg N [iterations]
-    [f32|f64]``: run that many Jacobi-CG iterations on the clamped brick (workload
-    drivers for profiling)."""
-    import sys
-
-    from . import _lib
-    from .materials import LinearElastic
-
-    args = list(sys.argv[1:] if argv is None else argv)
-    name = args[0] if args else "brick"
-    n = int(args[1]) if len(args) > 1 else 64
-    reps = int(args[2]) if len(args) > 2 else 3
-    dtype = torch.float64 if (len(args) > 3 and args[3] == "f64") else torch.float32
-    if name == "brick-cg":
-        import time
-
-        from . import solvers
-
-        P = clamped_brick(n, "cuda")
-        it = reps
-        b = P["b"].to(dtype)
-        solvers.cg(P["energy"], b, fixed=P["fixed"], dtype=dtype, rtol=1e-30, maxiter=it,
-                   check_every=min(it, 50), raise_on_fail=False)  # warm-up, graph build
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = solvers.cg(P["energy"], b, fixed=P["fixed"], dtype=dtype, rtol=1e-30, maxiter=it,
-                       check_every=min(it, 50), raise_on_fail=False)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        print(name, n, P["energy"].n_dofs, r.iterations, f"{1e6 * dt / max(r.iterations, 1):.1f} us/it")
-        return
-    if name == "brick":
-        P = clamped_brick(n, "cuda")
-        en, u = P["energy"], None
-    else:
-        P = stretched_kuhn(n, "cuda")
-        en = P["energy"] if name == "kuhn" else LinearElastic(P["op"], 1.0, 1.0)
-        u = None if name != "kuhn" else torch.zeros(en.n_dofs, dtype=dtype, device="cuda")
-    v = torch.ones(en.n_dofs, dtype=dtype, device="cuda")
-    y = torch.empty_like(v)
-    for _ in range(reps):
-        en.apply(_lib.TG_MODE_HVP, u, v, out=y)
-    torch.cuda.synchronize()
-    print(name, n, en.n_dofs, float(y.abs().sum()))
-
-
-if __name__ == "__main__":
-    _main()

@@ -28,7 +28,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._device import prec_of, ptr, require_cuda, workspace
+from ._device import aligned16, prec_of, ptr, require_cuda, workspace
 
 
 @dataclass
@@ -83,7 +83,7 @@ def cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None, fixed
     dtype = dtype or b.dtype
     require_cuda(b)
     n = energy.n_dofs
-    bb = b.reshape(-1).to(dtype).contiguous()
+    bb = aligned16(b.reshape(-1).to(dtype).contiguous())
     x = (x0.reshape(-1).to(dtype).clone() if x0 is not None
          else torch.zeros(n, dtype=dtype, device=b.device))
     desc, keep = energy.operator_desc(u, fixed, dtype)
@@ -110,7 +110,7 @@ def mixed_cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None,
     """FP32 inner CG + FP64 iterative refinement to ||b - A64 x|| <= rtol ||b||."""
     require_cuda(b)
     n = energy.n_dofs
-    bb = b.reshape(-1).to(torch.float64).contiguous()
+    bb = aligned16(b.reshape(-1).to(torch.float64).contiguous())
     x = (x0.reshape(-1).to(torch.float64).clone() if x0 is not None
          else torch.zeros(n, dtype=torch.float64, device=b.device))
     d64, k64 = energy.operator_desc(u, fixed, torch.float64)
@@ -175,7 +175,7 @@ def csr_cg(cm, b: torch.Tensor, x0=None, *, fixed=None, rtol: float = 1e-8,
             data = data.clone()
             _lib.call("tg_csr_apply_dirichlet", prec_of(dtype), n, ptr(cm.indptr),
                       ptr(cm.indices), ptr(mask), ptr(data), torch.cuda.current_stream().cuda_stream)
-    bb = b.reshape(-1).to(dtype).contiguous()
+    bb = aligned16(b.reshape(-1).to(dtype).contiguous())
     x = (x0.reshape(-1).to(dtype).clone() if x0 is not None
          else torch.zeros(n, dtype=dtype, device=b.device))
     diag = torch.empty(n, dtype=dtype, device=b.device)

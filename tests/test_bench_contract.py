@@ -39,17 +39,23 @@ def _check_base(d):
 
 
 def test_reference_arm_json():
-    d = _run(["--impl", "reference", "--steps", "1", "--warmup", "0"], timeout=600)
+    d = _run(["--impl", "reference", "--steps", "1", "--warmup", "0", "--size", "16"],
+             timeout=600)
     _check_base(d)
     assert d["impl"] == "reference" and d["cpu_baseline"]["kind"] in ("port", "reference")
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["value"] > 0
+    assert d["unit"] == "solves/s" and d["dtype"] == "f64"
+    assert d["config"]["cells_per_side"] == 16 and d["config"]["rtol"] == 1e-10
 
 
 @pytest.mark.gpu
 def test_gpu_arm_json(cuda):
-    d = _run(["--steps", "3", "--warmup", "3", "--batched", "0", "--serving", "0",
-              "--newton", "0", "--solve", "0", "--cpu-seconds", "1"], timeout=900)
+    d = _run(["--steps", "2", "--warmup", "3", "--batched", "0", "--serving", "0",
+              "--newton", "0", "--size", "32", "--fp64-solves", "1", "--cpu-iterations", "1"],
+             timeout=900)
     _check_base(d)
+    assert d["unit"] == "solves/s" and d["converged"] and d["rel_res"] <= 1e-10
+    assert d["fp64_solve"]["converged"] and d["fp64_solve"]["rel_res"] <= 1e-10
     rf = d["roofline"]
     assert rf["bound"] == "hbm" and rf["unit"] == "GB/s" and 0 < rf["frac"] < 1.5
     assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-9

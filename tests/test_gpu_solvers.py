@@ -160,3 +160,48 @@ def test_newton_neo_hookean_stretch(cuda):
     r = omat.residual(oo, omat.NeoHookean(1.0, 10.0), u.cpu().numpy())
     r[dofs] = 0
     assert np.linalg.norm(r) < 1e-9
+
+
+def test_solvers_accept_right_hand_sides_at_odd_offsets(cuda):
+    """A right-hand side that is a slice of a larger buffer (data at an offset that is
+    not a multiple of 16 bytes) is copied by the wrappers; the C ABI refuses such a
+    pointer on the host, before any launch, with TG_ERR_VALUE."""
+    import ctypes
+
+    from tatva_gb300 import _lib
+    from tatva_gb300._device import ptr, workspace
+
+    c, e, op, en, fixed, b = _brick_problem(4, cuda)
+    n = en.n_dofs
+    big = torch.zeros(n + 1, dtype=torch.float64, device=cuda)
+    big[1:] = b
+    b_odd = big[1:]
+    assert b_odd.data_ptr() % 16 != 0
+    r_ref = solvers.cg(en, b, fixed=fixed, rtol=1e-10)
+    r_odd = solvers.cg(en, b_odd, fixed=fixed, rtol=1e-10)
+    assert r_odd.converged and torch.equal(r_odd.x, r_ref.x)
+    m_ref = solvers.mixed_cg(en, b, fixed=fixed, rtol=1e-10)
+    m_odd = solvers.mixed_cg(en, b_odd, fixed=fixed, rtol=1e-10)
+    assert m_odd.converged and torch.equal(m_odd.x, m_ref.x)
+    # the raw entry points: refused on the host (no kernel runs)
+    desc, keep = en.operator_desc(None, fixed, torch.float64)
+    x_odd = torch.zeros(n + 1, dtype=torch.float64, device=cuda)[1:]
+    diag = torch.ones(n, dtype=torch.float64, device=cuda)
+    nb = _lib.lib().tg_cg_workspace_bytes(ctypes.byref(desc))
+    ws = workspace(nb, cuda)
+    st = _lib.SolveStats()
+    rc = _lib.lib().tg_cg_solve(ctypes.byref(desc), ptr(b_odd), ptr(torch.zeros_like(b)),
+                                ptr(diag), 1e-10, 10, 5, ptr(ws), nb, ctypes.byref(st),
+                                torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.TG_ERR_VALUE and "16-byte aligned" in _lib.lib().tg_last_error().decode()
+    rc = _lib.lib().tg_cg_solve(ctypes.byref(desc), ptr(b), ptr(x_odd), ptr(diag), 1e-10, 10, 5,
+                                ptr(ws), nb, ctypes.byref(st),
+                                torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.TG_ERR_VALUE
+    out = torch.zeros(1, dtype=torch.float64, device=cuda)
+    dws = workspace(_lib.lib().tg_dot_workspace_bytes(), cuda)
+    rc = _lib.lib().tg_dot(_lib.TG_F64, ptr(b_odd), ptr(b), n, ptr(out), ptr(dws),
+                           _lib.lib().tg_dot_workspace_bytes(),
+                           torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.TG_ERR_VALUE
+    del keep

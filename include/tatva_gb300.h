@@ -169,6 +169,13 @@ typedef struct tg_block_plan {
                                     corner a at (i,j,k) + (0,0,0) (1,0,0) (1,1,0)
                                     (0,1,0) (0,0,1) (1,0,1) (1,1,1) (0,1,1); 0: none */
   int32_t reserved0;
+  /* Hex8 structured brick (tg_grid_detect): nodes per axis Nx, Ny, Nz with node id
+   * i + Nx (j + Ny k), uniform spacing grid_h along each axis, one element per cell
+   * in the reference corner order.  Linear-elastic residual / HVP then run as a
+   * stencil over the grid (no element data read).  grid_nodes[0] = 0: not a brick. */
+  int32_t grid_nodes[3];
+  int32_t grid_reserved;
+  double grid_h[3];
 } tg_block_plan;
 
 /* Material parameters.  kind = TG_POISSON: p0 = kappa, p1 = f (source);
@@ -200,6 +207,15 @@ TG_API int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t* bl
                    int32_t* lnode_smem, int32_t* shared_node, int32_t* shared_ptr,
                    int32_t* shared_slots);
 TG_API void tg_plan_free(void* handle);
+/* HOST: is a Hex8 mesh a structured brick?  nodes[3] = (Nx, Ny, Nz) and h[3] = the
+ * spacing per axis when node n sits at (X[i], Y[j], Z[k]) for n = i + Nx (j + Ny k),
+ * the spacing along each axis is uniform (to 1e-13 relative), and the elements are the
+ * (Nx-1)(Ny-1)(Nz-1) cells, each once, with the corner order of the reference
+ * Hexahedron8 (tatva/element/base.py:478-491); nodes = (0, 0, 0) otherwise.  The
+ * result goes into tg_block_plan.grid_nodes / grid_h.  No reference counterpart: it
+ * selects the stencil schedule of the same HVP (jax.jvp(jax.grad(E)), README.md:93). */
+TG_API int tg_grid_detect(int elem, const int32_t* conn, int64_t n_elems, int64_t n_nodes,
+                          const double* coords, int dim, int32_t* nodes, double* h);
 /* Fill box_geom32 (device, 3 * n_elems floats) from FP32 coordinates and the int32
  * connectivity; identical in every bit to what the kernel derives from coordinates. */
 TG_API int tg_plan_box_geometry(const tg_block_plan* plan, const float* coords, const int32_t* conn,

@@ -66,6 +66,9 @@ class BlockPlan(ctypes.Structure):
         ("box_geom32", c_void_p),
         ("n_lattice_blocks", c_int32),
         ("reserved0", c_int32),
+        ("grid_nodes", c_int32 * 3),
+        ("grid_reserved", c_int32),
+        ("grid_h", c_double * 3),
     ]
 
 
@@ -154,6 +157,7 @@ SIGNATURES = {
     "tg_plan_sizes": (I, [P, P]),
     "tg_plan_export": (I, [P] + [P] * 12),
     "tg_plan_free": (None, [P]),
+    "tg_grid_detect": (I, [I, P, L, L, P, I, P, P]),
     "tg_plan_box_geometry": (I, [P, P, P, P, P]),
     "tg_apply_workspace_bytes": (S, [I, I, I, P]),
     "tg_apply": (I, [I, I, I, P, P, P, L, P, P, P, P, P, S, P]),

@@ -1031,6 +1031,17 @@ extern "C" int tg_apply(int elem, int prec, int mode, const tg_material* mat,
             const int n_aff = HasAffinePath<ET, MAT, MODE>::value ? plan->n_affine_blocks : 0;
             if (n_aff < 0 || n_aff > plan->n_blocks)
               return set_error(TG_ERR_VALUE, "plan.n_affine_blocks out of range");
+            if constexpr (ET == TG_HEX8 && MAT == TG_LINEAR_ELASTIC &&
+                          (MODE == TG_MODE_HVP || MODE == TG_MODE_RESIDUAL)) {
+              // structured brick: the stencil schedule over the grid
+              if (plan->grid_nodes[0] > 0 && mat->elem_param == nullptr &&
+                  (int64_t)plan->grid_nodes[0] * plan->grid_nodes[1] * plan->grid_nodes[2] ==
+                      n_nodes) {
+                const int rcg = launch_grid_le(plan, prec, MODE, u, v, fixed, y, mat->p0,
+                                               mat->p1, st);
+                if (rcg != TG_ERR_UNSUPPORTED) return rcg;
+              }
+            }
             if constexpr (HasAffinePath<ET, MAT, MODE>::value) {
               bool done = false;
               if constexpr (std::is_same<T, float>::value && MAT == TG_LINEAR_ELASTIC) {

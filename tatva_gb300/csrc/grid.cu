@@ -1,0 +1,437 @@
+// Linear-elastic Hex8 residual / HVP on a structured brick: the assembled operator as
+// a 27-point stencil of 3 x 3 blocks.
+//
+// When the mesh is a tensor grid of Nx x Ny x Nz nodes with uniform spacing (hx, hy,
+// hz) along each axis, node ids i + Nx (j + Ny k) and one element per cell with the
+// corner order of the reference Hexahedron8 (tatva/element/base.py:478-491), every
+// element has the same stiffness matrix and the HVP y = sum_e K_e v_e is, at a node
+// whose eight surrounding cells all exist, a fixed stencil.  With 1-D factors on an
+// axis of spacing h
+//   K(0) = 2/h, K(+-1) = -1/h          (int phi_n' phi_m')
+//   M(0) = 2h/3, M(+-1) = h/6          (int phi_n phi_m)
+//   G(d) = -d/2                        (int phi_n' phi_{n+d})
+// the 3 x 3 block for an input node at offset d = (dx, dy, dz) is
+//   C_aa(d) = mu (Kx My Mz + Mx Ky Mz + Mx My Kz)(d) + (lambda + mu) D_aa(d),
+//             D_xx = Kx My Mz, D_yy = Mx Ky Mz, D_zz = Mx My Kz,
+//   C_ab(d) = -(lambda + mu) G(d_a) G(d_b) M(d_c)      (a != b, c the third axis),
+// i.e. mu delta_ab sum_i D_ii + lambda D_ab + mu D_ba of the energy
+// 1/2 sigma:eps (tests/test_sparse_benchmark.py:30-78), integrated exactly -- the
+// 2 x 2 x 2 Gauss rule of the element is exact for these products -- so the stencil
+// equals the element-by-element sum up to rounding.  This is what jax.jvp(jax.grad(E))
+// computes for E = integrate(psi(grad u)) (README.md:93, tatva/sparse/base.py:257-265).
+//
+// Schedule (one launch):
+//   * interior CTAs: a tile of 32 x 8 node columns (x, y) and a run of z planes.  Each
+//     thread owns one column and sweeps z; the input plane (with a one-node halo, 34 x
+//     10 nodes, 3 components in a 16-byte slot) sits in shared memory; a plane adds its
+//     contributions to the outputs at z - 1, z, z + 1 (three accumulator sets), so each
+//     output is complete after its upper neighbour plane.  Planes arrive through
+//     registers two planes ahead (the Dirichlet mask is applied on the way) and are
+//     double-buffered in shared memory: one barrier per plane.  Per node and plane:
+//     nine 16-byte shared loads and ~90 FP operations, using the stencil's symmetries
+//     (in-plane sums grouped by |dx|, |dy| for the diagonal blocks; signed cross sums
+//     for the off-diagonal ones).
+//   * boundary CTAs: the nodes on the six faces, one per thread, as the sum over the
+//     cells that exist around the node of the element matrix (24 x 24, staged in
+//     shared memory) times the cell's input values.
+// Every output is written once by the thread that owns it, in a fixed order: the
+// result is deterministic and needs no atomics, partial slots or second pass.
+#include "tg_common.cuh"
+#include "tg_internal.h"
+
+namespace tg {
+
+constexpr int GR_TX = 32, GR_TY = 8, GR_THREADS = GR_TX * GR_TY;
+constexpr int GR_PX = GR_TX + 2, GR_PY = GR_TY + 2, GR_PLANE = GR_PX * GR_PY;  // 340
+constexpr int GR_SLOTS = (GR_PLANE + GR_THREADS - 1) / GR_THREADS;            // 2
+
+template <class T>
+struct GridCoef {
+  T c[3][8];   // diagonal blocks: c[a][ix + 2 iy + 4 iz], i* = |d*| in {0, 1}
+  T qxy[2];    // -(lambda + mu)/4 M_z(0), M_z(1)
+  T qxz[2];    // -(lambda + mu)/4 M_y(0), M_y(1)
+  T qyz[2];    // -(lambda + mu)/4 M_x(0), M_x(1)
+  T ke[8][8][3][3];  // element matrix, corners cn, cm = lx + 2 ly + 4 lz
+  int nx, ny, nz;    // nodes per axis
+  int tiles_x, tiles_y, tiles_z, tz;  // interior tiling: tz planes per tile
+  int n_interior_ctas;
+  int64_t n_boundary;
+};
+
+template <class T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  using type = float4;
+};
+template <>
+struct Vec4<double> {
+  using type = double4;
+};
+
+template <class T>
+__device__ __forceinline__ typename Vec4<T>::type make4(T a, T b, T c) {
+  typename Vec4<T>::type r;
+  r.x = a;
+  r.y = b;
+  r.z = c;
+  r.w = T(0);
+  return r;
+}
+
+// input value of dof (node g, comp d): v read as 0 on fixed dofs when MASK
+template <class T, bool MASK>
+__device__ __forceinline__ T load_in(const T* __restrict__ in, const uint8_t* __restrict__ fixed,
+                                     int64_t dof) {
+  T x = __ldg(in + dof);
+  if (MASK && __ldg(fixed + dof)) x = T(0);
+  return x;
+}
+
+// Interior tile: thread (lx, ly) owns node column (x0 + lx, y0 + ly), planes
+// [zs, ze) of output.
+template <class T, int MODE, bool MASK>
+__device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restrict__ in,
+                              const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
+                              T* __restrict__ y, typename Vec4<T>::type* sm) {
+  using V4 = typename Vec4<T>::type;
+  const int tid = threadIdx.x;
+  const int nx = P.nx, ny = P.ny, nz = P.nz;
+  const int tx = item % P.tiles_x;
+  const int rest = item / P.tiles_x;
+  const int ty = rest % P.tiles_y;
+  const int tzi = rest / P.tiles_y;
+  const int x0 = 1 + tx * GR_TX, y0 = 1 + ty * GR_TY;
+  const int zs = 1 + tzi * P.tz;
+  const int ze = min(zs + P.tz, nz - 1);
+  const int lx = tid % GR_TX, ly = tid / GR_TX;
+  const int x = x0 + lx, yy = y0 + ly;
+  const bool own = (x <= nx - 2) && (yy <= ny - 2);
+  const int64_t plane_nodes = (int64_t)nx * ny;
+
+  // staged slots of this thread: s = tid + k * GR_THREADS < GR_PLANE
+  int64_t soff[GR_SLOTS];  // node offset within a plane, -1: outside the grid / no slot
+#pragma unroll
+  for (int k = 0; k < GR_SLOTS; ++k) {
+    const int s = tid + k * GR_THREADS;
+    soff[k] = -1;
+    if (s < GR_PLANE) {
+      const int gx = x0 - 1 + s % GR_PX, gy = y0 - 1 + s / GR_PX;
+      if (gx < nx && gy < ny) soff[k] = gx + (int64_t)nx * gy;
+    }
+  }
+  auto load_plane = [&](int p, T (&r)[GR_SLOTS][3]) {
+#pragma unroll
+    for (int k = 0; k < GR_SLOTS; ++k) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) r[k][d] = T(0);
+      if (soff[k] >= 0 && p <= ze) {
+        const int64_t base = 3 * (soff[k] + plane_nodes * p);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) r[k][d] = load_in<T, MASK>(in, fixed, base + d);
+      }
+    }
+  };
+  auto store_plane = [&](V4* buf, const T (&r)[GR_SLOTS][3]) {
+#pragma unroll
+    for (int k = 0; k < GR_SLOTS; ++k) {
+      const int s = tid + k * GR_THREADS;
+      if (s < GR_PLANE) buf[s] = make4<T>(r[k][0], r[k][1], r[k][2]);
+    }
+  };
+
+  T accM[3], accP[3], accN[3];  // outputs at z - 1, z, z + 1 of the current plane z
+#pragma unroll
+  for (int a = 0; a < 3; ++a) accM[a] = accP[a] = accN[a] = T(0);
+  const int c0 = (lx + 1) + GR_PX * (ly + 1);
+
+  auto plane_step = [&](const V4* buf) {
+    // the nine in-plane neighbours, v[dy + 1][dx + 1]
+    V4 v[3][3];
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) v[dy][dx] = buf[c0 + (dx - 1) + GR_PX * (dy - 1)];
+    T g0[3], gx[3], gy[3], gc[3];
+    {
+      const T a0[3] = {v[1][1].x, v[1][1].y, v[1][1].z};
+      const T xm[3] = {v[1][0].x, v[1][0].y, v[1][0].z}, xp[3] = {v[1][2].x, v[1][2].y, v[1][2].z};
+      const T ym[3] = {v[0][1].x, v[0][1].y, v[0][1].z}, yp[3] = {v[2][1].x, v[2][1].y, v[2][1].z};
+      const T mm[3] = {v[0][0].x, v[0][0].y, v[0][0].z}, pm[3] = {v[0][2].x, v[0][2].y, v[0][2].z};
+      const T mp[3] = {v[2][0].x, v[2][0].y, v[2][0].z}, pp[3] = {v[2][2].x, v[2][2].y, v[2][2].z};
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        g0[b] = a0[b];
+        gx[b] = xm[b] + xp[b];
+        gy[b] = ym[b] + yp[b];
+        gc[b] = (mm[b] + mp[b]) + (pm[b] + pp[b]);
+      }
+      // diagonal blocks
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const T s0 = fma(P.c[a][3], gc[a], fma(P.c[a][2], gy[a], fma(P.c[a][1], gx[a], P.c[a][0] * g0[a])));
+        const T s1 = fma(P.c[a][7], gc[a], fma(P.c[a][6], gy[a], fma(P.c[a][5], gx[a], P.c[a][4] * g0[a])));
+        accP[a] += s0;
+        accM[a] += s1;
+        accN[a] += s1;
+      }
+      // x-y blocks: C = qxy(|dz|) dx dy (cross sum over the in-plane corners)
+      const T wx = (pp[0] + mm[0]) - (mp[0] + pm[0]);  // dx dy = +1 at (1,1), (-1,-1)
+      const T wy = (pp[1] + mm[1]) - (mp[1] + pm[1]);
+      accP[0] = fma(P.qxy[0], wy, accP[0]);
+      accM[0] = fma(P.qxy[1], wy, accM[0]);
+      accN[0] = fma(P.qxy[1], wy, accN[0]);
+      accP[1] = fma(P.qxy[0], wx, accP[1]);
+      accM[1] = fma(P.qxy[1], wx, accM[1]);
+      accN[1] = fma(P.qxy[1], wx, accN[1]);
+      // x-z blocks: C = qxz(|dy|) dx dz: odd in x, summed over dy with M_y
+      const T uz_x = fma(P.qxz[1], ((pm[2] - mm[2]) + (pp[2] - mp[2])), P.qxz[0] * (xp[2] - xm[2]));
+      const T ux_x = fma(P.qxz[1], ((pm[0] - mm[0]) + (pp[0] - mp[0])), P.qxz[0] * (xp[0] - xm[0]));
+      // y-z blocks: C = qyz(|dx|) dy dz: odd in y, summed over dx with M_x
+      const T uz_y = fma(P.qyz[1], ((mp[2] - mm[2]) + (pp[2] - pm[2])), P.qyz[0] * (yp[2] - ym[2]));
+      const T uy_y = fma(P.qyz[1], ((mp[1] - mm[1]) + (pp[1] - pm[1])), P.qyz[0] * (yp[1] - ym[1]));
+      // dz = plane - output: the output below (z - 1) sees dz = +1, the one above -1
+      accM[0] += uz_x;
+      accN[0] -= uz_x;
+      accM[2] += ux_x;
+      accN[2] -= ux_x;
+      accM[1] += uz_y;
+      accN[1] -= uz_y;
+      accM[2] += uy_y;
+      accN[2] -= uy_y;
+    }
+  };
+
+  auto emit = [&](int z, const T (&acc)[3]) {
+    if (!own || z < zs || z >= ze) return;
+    const int64_t base = 3 * (x + (int64_t)nx * yy + plane_nodes * z);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      T val = acc[d];
+      if (fixed && __ldg(fixed + base + d)) val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
+      y[base + d] = val;
+    }
+  };
+
+  V4* buf0 = sm;
+  V4* buf1 = sm + GR_PLANE;
+  T rA[GR_SLOTS][3], rB[GR_SLOTS][3];
+  // prologue: plane zs - 1 into buf0; zs in flight in rB, zs + 1 in rA
+  load_plane(zs - 1, rA);
+  store_plane(buf0, rA);
+  load_plane(zs, rB);
+  load_plane(zs + 1, rA);
+  __syncthreads();
+  // planes p = zs - 1 .. ze, two per trip: buf0 holds p, buf1 gets p + 1
+  for (int p = zs - 1; p <= ze; p += 2) {
+    plane_step(buf0);
+    emit(p - 1, accM);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      accM[a] = accP[a];
+      accP[a] = accN[a];
+      accN[a] = T(0);
+    }
+    store_plane(buf1, rB);
+    load_plane(p + 3, rB);
+    __syncthreads();
+    if (p + 1 > ze) break;
+    plane_step(buf1);
+    emit(p, accM);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      accM[a] = accP[a];
+      accP[a] = accN[a];
+      accN[a] = T(0);
+    }
+    store_plane(buf0, rA);
+    load_plane(p + 4, rA);
+    __syncthreads();
+  }
+}
+
+// Boundary node t of the six faces: z = 0 and z = nz - 1 (all nx ny nodes), y = 0 and
+// y = ny - 1 (nx (nz - 2)), x = 0 and x = nx - 1 ((ny - 2)(nz - 2)).
+__device__ __forceinline__ void boundary_node(int64_t t, int nx, int ny, int nz, int& x, int& y,
+                                              int& z) {
+  const int64_t fz = (int64_t)nx * ny, fy = (int64_t)nx * (nz - 2);
+  if (t < 2 * fz) {
+    z = t < fz ? 0 : nz - 1;
+    const int64_t r = t < fz ? t : t - fz;
+    x = (int)(r % nx);
+    y = (int)(r / nx);
+    return;
+  }
+  t -= 2 * fz;
+  if (t < 2 * fy) {
+    y = t < fy ? 0 : ny - 1;
+    const int64_t r = t < fy ? t : t - fy;
+    x = (int)(r % nx);
+    z = 1 + (int)(r / nx);
+    return;
+  }
+  t -= 2 * fy;
+  const int64_t fx = (int64_t)(ny - 2) * (nz - 2);
+  x = t < fx ? 0 : nx - 1;
+  const int64_t r = t < fx ? t : t - fx;
+  y = 1 + (int)(r % (ny - 2));
+  z = 1 + (int)(r / (ny - 2));
+}
+
+template <class T, int MODE, bool MASK>
+__device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restrict__ in,
+                              const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
+                              T* __restrict__ y, T* ke) {
+  for (int i = threadIdx.x; i < 8 * 8 * 9; i += blockDim.x) ke[i] = (&P.ke[0][0][0][0])[i];
+  __syncthreads();
+  const int64_t t = t0 + threadIdx.x;
+  if (t >= P.n_boundary) return;
+  const int nx = P.nx, ny = P.ny, nz = P.nz;
+  int x, yy, z;
+  boundary_node(t, nx, ny, nz, x, yy, z);
+  T acc[3] = {T(0), T(0), T(0)};
+  for (int o = 0; o < 8; ++o) {  // cell whose corner o is this node
+    const int ox = o & 1, oy = (o >> 1) & 1, oz = o >> 2;
+    const int cx = x - ox, cy = yy - oy, cz = z - oz;
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= nx - 1 || cy >= ny - 1 || cz >= nz - 1) continue;
+    const T* kr = ke + o * 72;  // rows of corner o: [cm][a][b]
+#pragma unroll 2
+    for (int cm = 0; cm < 8; ++cm) {
+      const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
+                                                         (int64_t)ny * (cz + (cm >> 2)));
+      const T v0 = load_in<T, MASK>(in, fixed, 3 * g);
+      const T v1 = load_in<T, MASK>(in, fixed, 3 * g + 1);
+      const T v2 = load_in<T, MASK>(in, fixed, 3 * g + 2);
+      const T* k9 = kr + cm * 9;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a] = fma(k9[3 * a + 2], v2, fma(k9[3 * a + 1], v1, fma(k9[3 * a], v0, acc[a])));
+    }
+  }
+  const int64_t base = 3 * (x + (int64_t)nx * (yy + (int64_t)ny * z));
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    T val = acc[d];
+    if (fixed && __ldg(fixed + base + d)) val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
+    y[base + d] = val;
+  }
+}
+
+template <class T, int MODE, bool MASK>
+__global__ void __launch_bounds__(GR_THREADS)
+    grid_le_kernel(const __grid_constant__ GridCoef<T> P, const T* __restrict__ in,
+                   const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
+                   T* __restrict__ y) {
+  using V4 = typename Vec4<T>::type;
+  __shared__ V4 sm[2 * GR_PLANE];
+  const int b = blockIdx.x;
+  if (b < P.n_interior_ctas) {
+    grid_interior<T, MODE, MASK>(P, b, in, vin, fixed, y, sm);
+  } else {
+    grid_boundary<T, MODE, MASK>(P, (int64_t)(b - P.n_interior_ctas) * GR_THREADS, in, vin,
+                                 fixed, y, reinterpret_cast<T*>(sm));
+  }
+}
+
+// ------------------------------------------------------------------------- host
+// Stencil coefficients and the element matrix from the spacings and Lame parameters,
+// in FP64, then rounded to T.
+template <class T>
+static void grid_coefficients(const double h[3], double mu, double lam, GridCoef<T>& P) {
+  double K[3][2], M[3][2];
+  for (int k = 0; k < 3; ++k) {
+    K[k][0] = 2.0 / h[k];
+    K[k][1] = -1.0 / h[k];
+    M[k][0] = 2.0 * h[k] / 3.0;
+    M[k][1] = h[k] / 6.0;
+  }
+  for (int i = 0; i < 8; ++i) {
+    const int ix = i & 1, iy = (i >> 1) & 1, iz = i >> 2;
+    const double D[3] = {K[0][ix] * M[1][iy] * M[2][iz], M[0][ix] * K[1][iy] * M[2][iz],
+                         M[0][ix] * M[1][iy] * K[2][iz]};
+    const double L = D[0] + D[1] + D[2];
+    for (int a = 0; a < 3; ++a) P.c[a][i] = (T)(mu * L + (lam + mu) * D[a]);
+  }
+  const double q = -(lam + mu) / 4.0;
+  for (int s = 0; s < 2; ++s) {
+    P.qxy[s] = (T)(q * M[2][s]);
+    P.qxz[s] = (T)(q * M[1][s]);
+    P.qyz[s] = (T)(q * M[0][s]);
+  }
+  // element matrix of one cell: corners cn, cm = lx + 2 ly + 4 lz; per axis the
+  // element-level 1-D integrals Kel = [[1,-1],[-1,1]]/h, Mel = h[[1/3,1/6],[1/6,1/3]],
+  // Gel(A, B) = int phi_A' phi_B = s_A / 2 (s = -1 at the lower corner, +1 upper)
+  for (int cn = 0; cn < 8; ++cn)
+    for (int cm = 0; cm < 8; ++cm) {
+      int ln[3], lm[3];
+      for (int k = 0; k < 3; ++k) {
+        ln[k] = (cn >> k) & 1;
+        lm[k] = (cm >> k) & 1;
+      }
+      auto DE = [&](int i, int j) {
+        double v = 1.0;
+        for (int k = 0; k < 3; ++k) {
+          double f;
+          if (i == j && j == k) f = (ln[k] == lm[k] ? 1.0 : -1.0) / h[k];
+          else if (k == i) f = (ln[k] ? 0.5 : -0.5);
+          else if (k == j) f = (lm[k] ? 0.5 : -0.5);
+          else f = h[k] * (ln[k] == lm[k] ? 1.0 / 3.0 : 1.0 / 6.0);
+          v *= f;
+        }
+        return v;
+      };
+      const double Ls = DE(0, 0) + DE(1, 1) + DE(2, 2);
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          P.ke[cn][cm][a][b] = (T)(lam * DE(a, b) + mu * DE(b, a) + (a == b ? mu * Ls : 0.0));
+    }
+}
+
+template <class T>
+static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, const T* v,
+                            const uint8_t* fixed, T* y, double mu, double lam,
+                            cudaStream_t st) {
+  GridCoef<T> P;
+  const int nx = plan->grid_nodes[0], ny = plan->grid_nodes[1], nz = plan->grid_nodes[2];
+  grid_coefficients<T>(plan->grid_h, mu, lam, P);
+  P.nx = nx;
+  P.ny = ny;
+  P.nz = nz;
+  // interior planes per tile: about four tiles per resident CTA slot over the grid
+  const int ix = nx - 2, iy = ny - 2, iz = nz - 2;
+  P.tiles_x = ix > 0 ? (ix + GR_TX - 1) / GR_TX : 0;
+  P.tiles_y = iy > 0 ? (iy + GR_TY - 1) / GR_TY : 0;
+  P.tz = 16;
+  P.tiles_z = iz > 0 ? (iz + P.tz - 1) / P.tz : 0;
+  const int64_t n_int = (int64_t)P.tiles_x * P.tiles_y * P.tiles_z;
+  P.n_boundary = (int64_t)nx * ny * nz - (int64_t)(ix > 0 ? ix : 0) * (iy > 0 ? iy : 0) *
+                                             (iz > 0 ? iz : 0);
+  const int64_t n_bnd_ctas = (P.n_boundary + GR_THREADS - 1) / GR_THREADS;
+  if (n_int + n_bnd_ctas > 0x7fffffff) return set_error(TG_ERR_VALUE, "grid too large");
+  P.n_interior_ctas = (int)n_int;
+  const T* in = (mode == TG_MODE_HVP) ? v : u;
+  const unsigned grid = (unsigned)(n_int + n_bnd_ctas);
+  if (grid == 0) return TG_OK;
+  if (mode == TG_MODE_HVP) {
+    if (fixed)
+      grid_le_kernel<T, TG_MODE_HVP, true><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
+    else
+      grid_le_kernel<T, TG_MODE_HVP, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
+  } else {
+    grid_le_kernel<T, TG_MODE_RESIDUAL, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
+  }
+  return launch_check("grid linear-elastic kernel");
+}
+
+int launch_grid_le(const tg_block_plan* plan, int prec, int mode, const void* u, const void* v,
+                   const uint8_t* fixed, void* y, double mu, double lam, cudaStream_t st) {
+  if (mode != TG_MODE_HVP && mode != TG_MODE_RESIDUAL) return TG_ERR_UNSUPPORTED;
+  if (plan->grid_nodes[0] < 2 || plan->grid_nodes[1] < 2 || plan->grid_nodes[2] < 2)
+    return TG_ERR_UNSUPPORTED;
+  if (prec == TG_F32)
+    return launch_grid_le_t<float>(plan, mode, (const float*)u, (const float*)v, fixed,
+                                   (float*)y, mu, lam, st);
+  return launch_grid_le_t<double>(plan, mode, (const double*)u, (const double*)v, fixed,
+                                  (double*)y, mu, lam, st);
+}
+
+}  // namespace tg

@@ -8,6 +8,7 @@
 // in-repo natural-order greedy restated here is the one this project reproduces
 // bit for bit.
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <new>
@@ -841,3 +842,67 @@ extern "C" int tg_plan_export(const void* handle, int32_t* blk_elem_ptr, int32_t
 }
 
 extern "C" void tg_plan_free(void* handle) { delete static_cast<Plan*>(handle); }
+
+// Structured-brick test of a Hex8 mesh (see tg_grid_detect in the header).
+extern "C" int tg_grid_detect(int elem, const int32_t* conn, int64_t n_elems, int64_t n_nodes,
+                              const double* coords, int dim, int32_t* nodes, double* h) {
+  if (!nodes || !h) return set_error(TG_ERR_VALUE, "tg_grid_detect: NULL output");
+  for (int d = 0; d < 3; ++d) {
+    nodes[d] = 0;
+    h[d] = 0.0;
+  }
+  if (elem != TG_HEX8 || dim != 3 || n_elems <= 0 || n_nodes < 8 || !conn || !coords)
+    return TG_OK;
+  // row length: nodes 0, 1, ... share y and z until the first row ends
+  const double* c = coords;
+  int64_t nx = 1;
+  while (nx < n_nodes && c[nx * 3 + 1] == c[1] && c[nx * 3 + 2] == c[2]) ++nx;
+  int64_t nxy = nx;
+  while (nxy < n_nodes && c[nxy * 3 + 2] == c[2]) nxy += nx;
+  if (nx < 2 || nxy % nx != 0 || n_nodes % nxy != 0) return TG_OK;
+  const int64_t ny = nxy / nx, nz = n_nodes / nxy;
+  if (ny < 2 || nz < 2 || nx > INT32_MAX || ny > INT32_MAX || nz > INT32_MAX) return TG_OK;
+  if ((nx - 1) * (ny - 1) * (nz - 1) != n_elems) return TG_OK;
+  // grid lines, strictly increasing with uniform spacing (1e-13 relative)
+  std::vector<double> X(nx), Y(ny), Z(nz);
+  for (int64_t i = 0; i < nx; ++i) X[i] = c[i * 3];
+  for (int64_t j = 0; j < ny; ++j) Y[j] = c[j * nx * 3 + 1];
+  for (int64_t k = 0; k < nz; ++k) Z[k] = c[k * nxy * 3 + 2];
+  double hh[3];
+  const std::vector<double>* lines[3] = {&X, &Y, &Z};
+  for (int d = 0; d < 3; ++d) {
+    const std::vector<double>& L = *lines[d];
+    const int64_t n = (int64_t)L.size();
+    hh[d] = (L[n - 1] - L[0]) / (double)(n - 1);
+    if (!(hh[d] > 0.0)) return TG_OK;
+    for (int64_t i = 0; i + 1 < n; ++i)
+      if (std::fabs((L[i + 1] - L[i]) - hh[d]) > 1e-13 * hh[d]) return TG_OK;
+  }
+  // every node on its grid position
+  for (int64_t k = 0; k < nz; ++k)
+    for (int64_t j = 0; j < ny; ++j)
+      for (int64_t i = 0; i < nx; ++i) {
+        const double* p = c + 3 * (i + nx * (j + ny * k));
+        if (p[0] != X[i] || p[1] != Y[j] || p[2] != Z[k]) return TG_OK;
+      }
+  // every cell exactly once, corners in the reference order
+  const int64_t off[8] = {0, 1, 1 + nx, nx, nxy, 1 + nxy, 1 + nx + nxy, nx + nxy};
+  std::vector<char> seen((size_t)n_elems, 0);
+  for (int64_t e = 0; e < n_elems; ++e) {
+    const int32_t* q = conn + e * 8;
+    const int64_t n0 = q[0];
+    if (n0 < 0 || n0 >= n_nodes) return TG_OK;
+    const int64_t i = n0 % nx, j = (n0 / nx) % ny, k = n0 / nxy;
+    if (i >= nx - 1 || j >= ny - 1 || k >= nz - 1) return TG_OK;
+    for (int a = 1; a < 8; ++a)
+      if ((int64_t)q[a] != n0 + off[a]) return TG_OK;
+    const int64_t cell = i + (nx - 1) * (j + (ny - 1) * k);
+    if (seen[cell]) return TG_OK;
+    seen[cell] = 1;
+  }
+  nodes[0] = (int32_t)nx;
+  nodes[1] = (int32_t)ny;
+  nodes[2] = (int32_t)nz;
+  for (int d = 0; d < 3; ++d) h[d] = hh[d];
+  return TG_OK;
+}

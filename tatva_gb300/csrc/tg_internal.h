@@ -16,4 +16,9 @@ int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords
                         const float* v, const uint8_t* fixed, float* y, float* partials,
                         float mu, float lam, cudaStream_t st);
 
+// Linear-elastic Hex8 residual / HVP on a structured brick (plan->grid_nodes set) as a
+// stencil over the grid; TG_ERR_UNSUPPORTED (nothing launched) for other modes or plans.
+int launch_grid_le(const tg_block_plan* plan, int prec, int mode, const void* u, const void* v,
+                   const uint8_t* fixed, void* y, double mu, double lam, cudaStream_t st);
+
 }  // namespace tg

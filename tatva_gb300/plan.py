@@ -82,6 +82,15 @@ class BlockPlan:
             setattr(s, k, self.dev[k].data_ptr())
         if np.array_equal(host["shared_slots"][:npart], np.arange(npart, dtype=np.int32)):
             s.shared_slots = None  # identity: the reduce reads partials in slot order
+        # structured brick: the linear-elastic residual / HVP run as a grid stencil
+        gn = (ctypes.c_int32 * 3)()
+        gh = (ctypes.c_double * 3)()
+        _lib.check(L.tg_grid_detect(elem_id, conn.ctypes.data, conn.shape[0], xyz.shape[0],
+                                    xyz.ctypes.data, xyz.shape[1], gn, gh))
+        self.grid_nodes = tuple(int(x) for x in gn)
+        self.grid_h = tuple(float(x) for x in gh)
+        s.grid_nodes[:] = self.grid_nodes
+        s.grid_h[:] = self.grid_h
         self.struct = s
         self.box_geom32 = None
         if elem_id == _lib.TG_HEX8 and ndiag > 0 and self.device.type == "cuda":
@@ -104,8 +113,19 @@ class BlockPlan:
     def ref(self):
         return ctypes.byref(self.struct)
 
+    @property
+    def grid(self) -> bool:
+        """True when the stencil schedule of a structured brick is in use."""
+        return self.struct.grid_nodes[0] > 0
+
+    @grid.setter
+    def grid(self, on: bool) -> None:
+        """Switch the structured-brick stencil schedule off (element blocks for every
+        mode) or back on, when the mesh is a brick."""
+        self.struct.grid_nodes[:] = self.grid_nodes if on else (0, 0, 0)
+
     def stats(self) -> dict:
         s = dict(self.sizes)
-        s.update(block_elems=self.block_elems, threads=self.threads,
+        s.update(block_elems=self.block_elems, threads=self.threads, grid=self.grid,
                  shared_fraction=self.sizes["n_partials"] / max(self.sizes["local_nodes"], 1))
         return s

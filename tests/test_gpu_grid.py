@@ -1,0 +1,112 @@
+"""The structured-brick stencil schedule of the linear-elastic Hex8 residual / HVP
+(``grid_le_kernel``) against the oracle and against the element-block kernels that
+the same plan runs with the stencil switched off.
+
+Tolerances (relative max-norm): FP64 <= 1e-12 against the oracle and <= 1e-13
+between the two FP64 schedules; FP32 <= 1e-5 against the FP64 oracle.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import elements as oe
+from oracle import materials as omat
+from oracle import mesh as om
+from oracle import operator as oop
+from tatva_gb300 import Mesh, Operator, element, materials
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-12
+SWAP64_TOL = 1e-13
+F32_TOL = 1e-5
+MU, LAM = 0.7, 1.9
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = b.detach().cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def _setup(shape, lengths, cuda, seed=0):
+    c, e = om.brick(*shape, lengths=lengths)
+    op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    en = materials.LinearElastic(op, MU, LAM)
+    assert en.plan().grid, en.plan().stats()
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal(en.n_dofs)
+    u = 0.01 * rng.standard_normal(en.n_dofs)
+    fixed = np.zeros(en.n_dofs, np.uint8)
+    fixed[rng.random(en.n_dofs) < 0.1] = 1  # scattered fixed dofs, not only whole nodes
+    fixed.reshape(-1, 3)[c[:, 0] == c[:, 0].min()] = 1  # and a clamped face
+    return c, e, en, v, u, fixed
+
+
+def _oracle(c, e, v, u, fixed):
+    oo = oop.OracleOperator(c, e, oe.Hexahedron8())
+    law = omat.LinearElastic(MU, LAM)
+    f = fixed.astype(bool)
+    yo = omat.hvp(oo, law, None, np.where(f, 0.0, v))
+    yo[f] = v[f]
+    ro = omat.residual(oo, law, u)
+    ro[f] = 0.0
+    return omat.hvp(oo, law, None, v), omat.residual(oo, law, u), yo, ro
+
+
+SHAPES = [((1, 1, 1), (1.0, 1.0, 1.0)),      # boundary CTAs only
+          ((2, 3, 4), (0.5, 0.9, 1.3)),      # one interior node layer in x
+          ((7, 5, 6), (0.7, 0.5, 1.2)),      # anisotropic spacing
+          ((33, 9, 17), (1.0, 0.3, 0.5)),    # partial tiles in x, y and z
+          ((40, 20, 36), (4.0, 2.0, 3.6))]   # several tiles per axis
+
+
+@pytest.mark.parametrize("shape,lengths", SHAPES)
+def test_grid_hvp_and_residual_fp64_fp32(cuda, shape, lengths):
+    c, e, en, v, u, fixed = _setup(shape, lengths, cuda)
+    yo, ro, yom, rom = _oracle(c, e, v, u, fixed)
+    f = torch.as_tensor(fixed, device=cuda)
+    for dtype, tol in ((torch.float64, F64_TOL), (torch.float32, F32_TOL)):
+        vt = torch.as_tensor(v, dtype=dtype, device=cuda)
+        ut = torch.as_tensor(u, dtype=dtype, device=cuda)
+        assert rel(en.hvp(None, vt), yo) < tol, dtype
+        assert rel(en.residual(ut), ro) < tol, dtype
+        assert rel(en.hvp(None, vt, fixed=f), yom) < tol, dtype
+        assert rel(en.residual(ut, fixed=f), rom) < tol, dtype
+
+
+def test_grid_matches_element_blocks_and_is_deterministic(cuda):
+    c, e, en, v, u, fixed = _setup((24, 17, 19), (2.4, 1.7, 1.9), cuda, seed=3)
+    plan = en.plan()
+    f = torch.as_tensor(fixed, device=cuda)
+    vt = torch.as_tensor(v, device=cuda)
+    a, b = en.hvp(None, vt, fixed=f), en.hvp(None, vt, fixed=f)
+    assert torch.equal(a, b)
+    plan.grid = False
+    try:
+        ref = en.hvp(None, vt, fixed=f)
+    finally:
+        plan.grid = True
+    assert rel(a, ref) < SWAP64_TOL
+    v32 = vt.float()
+    a32, b32 = en.hvp(None, v32), en.hvp(None, v32)
+    assert torch.equal(a32, b32)
+    assert rel(a32, en.hvp(None, vt)) < F32_TOL
+
+
+def test_grid_brick_128_properties(cuda):
+    """The 128^3 brick of the benchmark through the stencil: symmetry (w.Kv = v.Kw),
+    linearity and FP32 against FP64, at full size."""
+    c, e = om.brick(128, 128, 128)
+    op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    en = materials.LinearElastic.from_young(op, 1.0, 0.3)
+    assert en.plan().grid
+    g = torch.Generator(device=cuda).manual_seed(5)
+    v = torch.randn(en.n_dofs, dtype=torch.float64, device=cuda, generator=g)
+    w = torch.randn(en.n_dofs, dtype=torch.float64, device=cuda, generator=g)
+    kv, kw = en.hvp(None, v), en.hvp(None, w)
+    s1, s2 = float(w @ kv), float(v @ kw)
+    assert abs(s1 - s2) <= 1e-12 * (abs(s1) + abs(s2))
+    assert rel(en.hvp(None, 2.0 * v - 3.0 * w), 2.0 * kv - 3.0 * kw) < 1e-13
+    assert rel(en.hvp(None, v.float()), kv) < F32_TOL

@@ -42,6 +42,7 @@ def graded_brick(n, seed=0):
 def _run(c, e, cuda, fixed=None, block_elems=512):
     op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
     plan = op.plan(block_elems, 4096, 128)
+    plan.grid = False  # element blocks even where the mesh is a uniform brick
     en = materials.LinearElastic(op, 0.7, 1.9)
     en.use_plan(plan)
     rng = np.random.default_rng(3)
@@ -128,6 +129,7 @@ def test_lattice_many_blocks_per_cta_and_bitwise_repeat(cuda):
     c, e = om.brick(128, 64, 64)  # 1024 blocks, above the 608 resident CTAs of a GB300
     op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
     plan = op.plan(512, 4096, 128)
+    plan.grid = False  # a uniform brick: without this the stencil schedule runs it
     assert plan.sizes["n_lattice_blocks"] == plan.sizes["n_blocks"] == 1024
     en = materials.LinearElastic(op, 0.7, 1.9)
     en.use_plan(plan)

@@ -145,6 +145,18 @@ def test_hex_brick_affine_and_general(cuda, shape, jitter, kind):
     assert rel(en.hvp(_t(u, cuda), _t(v, cuda)), omat.hvp(oo, law, u, v)) < F64_TOL
     assert rel(en.hvp(_t(u, cuda, torch.float32), _t(v, cuda, torch.float32)),
                omat.hvp(oo, law, u, v)) < 1e-4
+    if kind == "linear_elastic" and not jitter:
+        # a uniform brick: the stencil schedule above; the modal element path here
+        plan = en.plan()
+        assert plan.grid
+        plan.grid = False
+        try:
+            assert rel(en.residual(_t(u, cuda)), omat.residual(oo, law, u)) < F64_TOL
+            assert rel(en.hvp(_t(u, cuda), _t(v, cuda)), omat.hvp(oo, law, u, v)) < F64_TOL
+            assert rel(en.hvp(_t(u, cuda, torch.float32), _t(v, cuda, torch.float32)),
+                       omat.hvp(oo, law, u, v)) < 1e-4
+        finally:
+            plan.grid = True
 
 
 def test_hex_box_geometry_path_is_bitwise_equal(cuda):

@@ -223,3 +223,49 @@ def test_lattice_blocks_of_structured_bricks(shape, n_lat, n_blocks):
     c2[np.argmin(np.linalg.norm(c2 - c2.mean(axis=0), axis=1))] += 0.01
     p2 = BlockPlan(_lib.TG_HEX8, e, c2, "cpu", block_elems=512, threads=128)
     assert p2.sizes["n_lattice_blocks"] < max(n_lat, 1)
+
+
+def _detect(c, e, elem=_lib.TG_HEX8):
+    gn = (ctypes.c_int32 * 3)()
+    gh = (ctypes.c_double * 3)()
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    e = np.ascontiguousarray(e, dtype=np.int32)
+    _lib.check(_lib.lib().tg_grid_detect(elem, e.ctypes.data, e.shape[0], c.shape[0],
+                                         c.ctypes.data, c.shape[1], gn, gh))
+    return tuple(gn), tuple(gh)
+
+
+def test_grid_detect_structured_bricks():
+    """Structured bricks (node id i + Nx (j + Ny k), uniform spacing per axis, each cell
+    once with the reference corner order) are recognised; anything else is not."""
+    c, e = om.brick(7, 5, 6, lengths=(0.7, 0.5, 1.2))
+    n, h = _detect(c, e)
+    assert n == (8, 6, 7) and np.allclose(h, (0.1, 0.1, 0.2), rtol=1e-14)
+    # element order does not matter
+    perm = np.random.default_rng(0).permutation(e.shape[0])
+    assert _detect(c, e[perm])[0] == (8, 6, 7)
+    # one cell: all nodes on the boundary
+    assert _detect(*om.brick(1, 1, 1))[0] == (2, 2, 2)
+    # not bricks: uneven spacing, jitter, renumbered nodes, rotated corner order,
+    # a missing or repeated cell, a Tet4 mesh
+    cg = c.copy()
+    cg[:, 0] = np.where(c[:, 0] > 0.35, c[:, 0] + 0.01 * (c[:, 0] - 0.35), c[:, 0])
+    assert _detect(cg, e)[0] == (0, 0, 0)
+    assert _detect(om.jitter_interior(c, 0.1, 0.2, seed=1), e)[0] == (0, 0, 0)
+    p = np.random.default_rng(1).permutation(c.shape[0])
+    inv = np.empty_like(p)
+    inv[p] = np.arange(p.size)
+    assert _detect(c[p], inv[e])[0] == (0, 0, 0)
+    assert _detect(c, np.roll(e, 1, axis=1))[0] == (0, 0, 0)
+    e2 = e.copy()
+    e2[3] = e2[4]
+    assert _detect(c, e2)[0] == (0, 0, 0)
+    ck, ek = om.kuhn_box((1, 1, 1), (3, 3, 3), origin=(0, 0, 0))
+    assert _detect(ck, ek, _lib.TG_TET4)[0] == (0, 0, 0)
+    # the plan carries the result, and can switch the stencil schedule off
+    plan = BlockPlan(_lib.TG_HEX8, e, c, "cpu")
+    assert plan.grid and tuple(plan.struct.grid_nodes) == (8, 6, 7)
+    plan.grid = False
+    assert not plan.grid and tuple(plan.struct.grid_nodes) == (0, 0, 0)
+    plan.grid = True
+    assert tuple(plan.struct.grid_nodes) == (8, 6, 7)

@@ -49,6 +49,7 @@ def _cases(cuda):
     # its partial slots in its own order, on scratch left behind by the other plans
     cl, el = om.brick(16, 8, 8)
     lat = Operator(Mesh(cl, el, device=cuda), element.Hexahedron8())
+    lat.plan().grid = False  # a uniform brick: keep the element blocks and their slots
     return [("hex8 box LE", materials.LinearElastic(box, 0.8, 1.3), c),
             ("hex8 jittered LE", materials.LinearElastic(jit, 0.8, 1.3), cj),
             ("tet4 NH", materials.NeoHookean(tet, 1.0, 10.0), ct),

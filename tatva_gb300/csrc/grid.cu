@@ -51,10 +51,11 @@ struct GridCoef {
   T qxy[2];    // -(lambda + mu)/4 M_z(0), M_z(1)
   T qxz[2];    // -(lambda + mu)/4 M_y(0), M_y(1)
   T qyz[2];    // -(lambda + mu)/4 M_x(0), M_x(1)
+  T r1[3];     // in-plane row sum of the |dz| = 1 diagonal-block coefficients
   T ke[8][8][3][3];  // element matrix, corners cn, cm = lx + 2 ly + 4 lz
   int nx, ny, nz;    // nodes per axis
   int tiles_x, tiles_y, tiles_z, tz;  // interior tiling: tz planes per tile
-  int n_interior_ctas;
+  int n_boundary_ctas;
   int64_t n_boundary;
 };
 
@@ -145,6 +146,13 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   for (int a = 0; a < 3; ++a) accM[a] = accP[a] = accN[a] = T(0);
   const int c0 = (lx + 1) + GR_PX * (ly + 1);
 
+  // Difference form: every block row of the stencil sums to zero (a rigid translation
+  // has no stiffness), so each in-plane neighbour enters as its difference to the
+  // column's value in that plane, and the column's own values enter as the second
+  // difference along z with the in-plane row sum R1 of the |dz| = 1 coefficients.
+  // For smooth fields this keeps the FP32 result as accurate as its rounded input
+  // allows (the value form loses a factor of ~1/h^2 to cancellation).
+  T prev[3];  // the column's value in the previous plane
   auto plane_step = [&](const V4* buf) {
     // the nine in-plane neighbours, v[dy + 1][dx + 1]
     V4 v[3][3];
@@ -152,54 +160,49 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
     for (int dy = 0; dy < 3; ++dy)
 #pragma unroll
       for (int dx = 0; dx < 3; ++dx) v[dy][dx] = buf[c0 + (dx - 1) + GR_PX * (dy - 1)];
-    T g0[3], gx[3], gy[3], gc[3];
-    {
-      const T a0[3] = {v[1][1].x, v[1][1].y, v[1][1].z};
-      const T xm[3] = {v[1][0].x, v[1][0].y, v[1][0].z}, xp[3] = {v[1][2].x, v[1][2].y, v[1][2].z};
-      const T ym[3] = {v[0][1].x, v[0][1].y, v[0][1].z}, yp[3] = {v[2][1].x, v[2][1].y, v[2][1].z};
-      const T mm[3] = {v[0][0].x, v[0][0].y, v[0][0].z}, pm[3] = {v[0][2].x, v[0][2].y, v[0][2].z};
-      const T mp[3] = {v[2][0].x, v[2][0].y, v[2][0].z}, pp[3] = {v[2][2].x, v[2][2].y, v[2][2].z};
+    const T a0[3] = {v[1][1].x, v[1][1].y, v[1][1].z};
+    const T xm[3] = {v[1][0].x, v[1][0].y, v[1][0].z}, xp[3] = {v[1][2].x, v[1][2].y, v[1][2].z};
+    const T ym[3] = {v[0][1].x, v[0][1].y, v[0][1].z}, yp[3] = {v[2][1].x, v[2][1].y, v[2][1].z};
+    const T mm[3] = {v[0][0].x, v[0][0].y, v[0][0].z}, pm[3] = {v[0][2].x, v[0][2].y, v[0][2].z};
+    const T mp[3] = {v[2][0].x, v[2][0].y, v[2][0].z}, pp[3] = {v[2][2].x, v[2][2].y, v[2][2].z};
+    // diagonal blocks: second differences grouped by |dx|, |dy|
 #pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        g0[b] = a0[b];
-        gx[b] = xm[b] + xp[b];
-        gy[b] = ym[b] + yp[b];
-        gc[b] = (mm[b] + mp[b]) + (pm[b] + pp[b]);
-      }
-      // diagonal blocks
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const T s0 = fma(P.c[a][3], gc[a], fma(P.c[a][2], gy[a], fma(P.c[a][1], gx[a], P.c[a][0] * g0[a])));
-        const T s1 = fma(P.c[a][7], gc[a], fma(P.c[a][6], gy[a], fma(P.c[a][5], gx[a], P.c[a][4] * g0[a])));
-        accP[a] += s0;
-        accM[a] += s1;
-        accN[a] += s1;
-      }
-      // x-y blocks: C = qxy(|dz|) dx dy (cross sum over the in-plane corners)
-      const T wx = (pp[0] + mm[0]) - (mp[0] + pm[0]);  // dx dy = +1 at (1,1), (-1,-1)
-      const T wy = (pp[1] + mm[1]) - (mp[1] + pm[1]);
-      accP[0] = fma(P.qxy[0], wy, accP[0]);
-      accM[0] = fma(P.qxy[1], wy, accM[0]);
-      accN[0] = fma(P.qxy[1], wy, accN[0]);
-      accP[1] = fma(P.qxy[0], wx, accP[1]);
-      accM[1] = fma(P.qxy[1], wx, accM[1]);
-      accN[1] = fma(P.qxy[1], wx, accN[1]);
-      // x-z blocks: C = qxz(|dy|) dx dz: odd in x, summed over dy with M_y
-      const T uz_x = fma(P.qxz[1], ((pm[2] - mm[2]) + (pp[2] - mp[2])), P.qxz[0] * (xp[2] - xm[2]));
-      const T ux_x = fma(P.qxz[1], ((pm[0] - mm[0]) + (pp[0] - mp[0])), P.qxz[0] * (xp[0] - xm[0]));
-      // y-z blocks: C = qyz(|dx|) dy dz: odd in y, summed over dx with M_x
-      const T uz_y = fma(P.qyz[1], ((mp[2] - mm[2]) + (pp[2] - pm[2])), P.qyz[0] * (yp[2] - ym[2]));
-      const T uy_y = fma(P.qyz[1], ((mp[1] - mm[1]) + (pp[1] - pm[1])), P.qyz[0] * (yp[1] - ym[1]));
-      // dz = plane - output: the output below (z - 1) sees dz = +1, the one above -1
-      accM[0] += uz_x;
-      accN[0] -= uz_x;
-      accM[2] += ux_x;
-      accN[2] -= ux_x;
-      accM[1] += uz_y;
-      accN[1] -= uz_y;
-      accM[2] += uy_y;
-      accN[2] -= uy_y;
+    for (int a = 0; a < 3; ++a) {
+      const T gx = (xm[a] - a0[a]) + (xp[a] - a0[a]);
+      const T gy = (ym[a] - a0[a]) + (yp[a] - a0[a]);
+      const T gc = ((mm[a] - a0[a]) + (mp[a] - a0[a])) + ((pm[a] - a0[a]) + (pp[a] - a0[a]));
+      const T s0 = fma(P.c[a][3], gc, fma(P.c[a][2], gy, P.c[a][1] * gx));
+      const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, P.c[a][5] * gx));
+      const T dz = a0[a] - prev[a];
+      accP[a] = fma(-P.r1[a], dz, accP[a] + s0);
+      accM[a] = fma(P.r1[a], dz, accM[a] + s1);
+      accN[a] += s1;
+      prev[a] = a0[a];
     }
+    // x-y blocks: C = qxy(|dz|) dx dy, the cross sum of the in-plane corners
+    const T wx = (pp[0] - pm[0]) - (mp[0] - mm[0]);
+    const T wy = (pp[1] - pm[1]) - (mp[1] - mm[1]);
+    accP[0] = fma(P.qxy[0], wy, accP[0]);
+    accM[0] = fma(P.qxy[1], wy, accM[0]);
+    accN[0] = fma(P.qxy[1], wy, accN[0]);
+    accP[1] = fma(P.qxy[0], wx, accP[1]);
+    accM[1] = fma(P.qxy[1], wx, accM[1]);
+    accN[1] = fma(P.qxy[1], wx, accN[1]);
+    // x-z blocks: C = qxz(|dy|) dx dz: odd in x, summed over dy with M_y
+    const T uz_x = fma(P.qxz[1], ((pm[2] - mm[2]) + (pp[2] - mp[2])), P.qxz[0] * (xp[2] - xm[2]));
+    const T ux_x = fma(P.qxz[1], ((pm[0] - mm[0]) + (pp[0] - mp[0])), P.qxz[0] * (xp[0] - xm[0]));
+    // y-z blocks: C = qyz(|dx|) dy dz: odd in y, summed over dx with M_x
+    const T uz_y = fma(P.qyz[1], ((mp[2] - mm[2]) + (pp[2] - pm[2])), P.qyz[0] * (yp[2] - ym[2]));
+    const T uy_y = fma(P.qyz[1], ((mp[1] - mm[1]) + (pp[1] - pm[1])), P.qyz[0] * (yp[1] - ym[1]));
+    // dz = plane - output: the output below (z - 1) sees dz = +1, the one above -1
+    accM[0] += uz_x;
+    accN[0] -= uz_x;
+    accM[2] += ux_x;
+    accN[2] -= ux_x;
+    accM[1] += uz_y;
+    accN[1] -= uz_y;
+    accM[2] += uy_y;
+    accN[2] -= uy_y;
   };
 
   auto emit = [&](int z, const T (&acc)[3]) {
@@ -222,6 +225,12 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   load_plane(zs, rB);
   load_plane(zs + 1, rA);
   __syncthreads();
+  {  // the first plane's step then sees no z difference (its outputs are discarded)
+    const V4 c = buf0[c0];
+    prev[0] = c.x;
+    prev[1] = c.y;
+    prev[2] = c.z;
+  }
   // planes p = zs - 1 .. ze, two per trip: buf0 holds p, buf1 gets p + 1
   for (int p = zs - 1; p <= ze; p += 2) {
     plane_step(buf0);
@@ -295,7 +304,7 @@ __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restr
     const int cx = x - ox, cy = yy - oy, cz = z - oz;
     if (cx < 0 || cy < 0 || cz < 0 || cx >= nx - 1 || cy >= ny - 1 || cz >= nz - 1) continue;
     const T* kr = ke + o * 72;  // rows of corner o: [cm][a][b]
-#pragma unroll 2
+#pragma unroll
     for (int cm = 0; cm < 8; ++cm) {
       const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
                                                          (int64_t)ny * (cz + (cm >> 2)));
@@ -323,12 +332,13 @@ __global__ void __launch_bounds__(GR_THREADS)
                    T* __restrict__ y) {
   using V4 = typename Vec4<T>::type;
   __shared__ V4 sm[2 * GR_PLANE];
+  // boundary CTAs first: they start with the first wave and overlap the interior tiles
   const int b = blockIdx.x;
-  if (b < P.n_interior_ctas) {
-    grid_interior<T, MODE, MASK>(P, b, in, vin, fixed, y, sm);
+  if (b < P.n_boundary_ctas) {
+    grid_boundary<T, MODE, MASK>(P, (int64_t)b * GR_THREADS, in, vin, fixed, y,
+                                 reinterpret_cast<T*>(sm));
   } else {
-    grid_boundary<T, MODE, MASK>(P, (int64_t)(b - P.n_interior_ctas) * GR_THREADS, in, vin,
-                                 fixed, y, reinterpret_cast<T*>(sm));
+    grid_interior<T, MODE, MASK>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm);
   }
 }
 
@@ -350,6 +360,16 @@ static void grid_coefficients(const double h[3], double mu, double lam, GridCoef
                          M[0][ix] * M[1][iy] * K[2][iz]};
     const double L = D[0] + D[1] + D[2];
     for (int a = 0; a < 3; ++a) P.c[a][i] = (T)(mu * L + (lam + mu) * D[a]);
+  }
+  for (int a = 0; a < 3; ++a) {
+    double r = 0.0;  // sum over dx, dy of c(dx, dy, 1): weights 1, 2, 2, 4 by class
+    for (int i = 4; i < 8; ++i) {
+      const int ix = i & 1, iy = (i >> 1) & 1;
+      const double D[3] = {K[0][ix] * M[1][iy] * M[2][1], M[0][ix] * K[1][iy] * M[2][1],
+                           M[0][ix] * M[1][iy] * K[2][1]};
+      r += (ix ? 2.0 : 1.0) * (iy ? 2.0 : 1.0) * (mu * (D[0] + D[1] + D[2]) + (lam + mu) * D[a]);
+    }
+    P.r1[a] = (T)r;
   }
   const double q = -(lam + mu) / 4.0;
   for (int s = 0; s < 2; ++s) {
@@ -407,7 +427,7 @@ static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, con
                                              (iz > 0 ? iz : 0);
   const int64_t n_bnd_ctas = (P.n_boundary + GR_THREADS - 1) / GR_THREADS;
   if (n_int + n_bnd_ctas > 0x7fffffff) return set_error(TG_ERR_VALUE, "grid too large");
-  P.n_interior_ctas = (int)n_int;
+  P.n_boundary_ctas = (int)n_bnd_ctas;
   const T* in = (mode == TG_MODE_HVP) ? v : u;
   const unsigned grid = (unsigned)(n_int + n_bnd_ctas);
   if (grid == 0) return TG_OK;

@@ -36,6 +36,8 @@
 //     shared memory) times the cell's input values.
 // Every output is written once by the thread that owns it, in a fixed order: the
 // result is deterministic and needs no atomics, partial slots or second pass.
+#include <type_traits>
+
 #include "tg_common.cuh"
 #include "tg_internal.h"
 
@@ -146,13 +148,14 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   for (int a = 0; a < 3; ++a) accM[a] = accP[a] = accN[a] = T(0);
   const int c0 = (lx + 1) + GR_PX * (ly + 1);
 
-  // Difference form: every block row of the stencil sums to zero (a rigid translation
+  // Difference form (FP32): every block row of the stencil sums to zero (a rigid translation
   // has no stiffness), so each in-plane neighbour enters as its difference to the
   // column's value in that plane, and the column's own values enter as the second
   // difference along z with the in-plane row sum R1 of the |dz| = 1 coefficients.
   // For smooth fields this keeps the FP32 result as accurate as its rounded input
   // allows (the value form loses a factor of ~1/h^2 to cancellation).
-  T prev[3];  // the column's value in the previous plane
+  constexpr bool DIFF = std::is_same<T, float>::value;
+  T prev[3];  // the column's value in the previous plane (difference form)
   auto plane_step = [&](const V4* buf) {
     // the nine in-plane neighbours, v[dy + 1][dx + 1]
     V4 v[3][3];
@@ -165,19 +168,30 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
     const T ym[3] = {v[0][1].x, v[0][1].y, v[0][1].z}, yp[3] = {v[2][1].x, v[2][1].y, v[2][1].z};
     const T mm[3] = {v[0][0].x, v[0][0].y, v[0][0].z}, pm[3] = {v[0][2].x, v[0][2].y, v[0][2].z};
     const T mp[3] = {v[2][0].x, v[2][0].y, v[2][0].z}, pp[3] = {v[2][2].x, v[2][2].y, v[2][2].z};
-    // diagonal blocks: second differences grouped by |dx|, |dy|
+    // diagonal blocks grouped by |dx|, |dy|: in FP32 as second differences (difference
+    // form), in FP64 from the values themselves (fewer operations on the FP64 pipe;
+    // no precision to win there)
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      const T gx = (xm[a] - a0[a]) + (xp[a] - a0[a]);
-      const T gy = (ym[a] - a0[a]) + (yp[a] - a0[a]);
-      const T gc = ((mm[a] - a0[a]) + (mp[a] - a0[a])) + ((pm[a] - a0[a]) + (pp[a] - a0[a]));
-      const T s0 = fma(P.c[a][3], gc, fma(P.c[a][2], gy, P.c[a][1] * gx));
-      const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, P.c[a][5] * gx));
-      const T dz = a0[a] - prev[a];
-      accP[a] = fma(-P.r1[a], dz, accP[a] + s0);
-      accM[a] = fma(P.r1[a], dz, accM[a] + s1);
-      accN[a] += s1;
-      prev[a] = a0[a];
+      if constexpr (DIFF) {
+        const T gx = (xm[a] - a0[a]) + (xp[a] - a0[a]);
+        const T gy = (ym[a] - a0[a]) + (yp[a] - a0[a]);
+        const T gc = ((mm[a] - a0[a]) + (mp[a] - a0[a])) + ((pm[a] - a0[a]) + (pp[a] - a0[a]));
+        const T s0 = fma(P.c[a][3], gc, fma(P.c[a][2], gy, P.c[a][1] * gx));
+        const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, P.c[a][5] * gx));
+        const T dz = a0[a] - prev[a];
+        accP[a] = fma(-P.r1[a], dz, accP[a] + s0);
+        accM[a] = fma(P.r1[a], dz, accM[a] + s1);
+        accN[a] += s1;
+        prev[a] = a0[a];
+      } else {
+        const T gx = xm[a] + xp[a], gy = ym[a] + yp[a];
+        const T gc = (mm[a] + mp[a]) + (pm[a] + pp[a]);
+        accP[a] = fma(P.c[a][3], gc, fma(P.c[a][2], gy, fma(P.c[a][1], gx, fma(P.c[a][0], a0[a], accP[a]))));
+        const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, fma(P.c[a][5], gx, P.c[a][4] * a0[a])));
+        accM[a] += s1;
+        accN[a] += s1;
+      }
     }
     // x-y blocks: C = qxy(|dz|) dx dy, the cross sum of the in-plane corners
     const T wx = (pp[0] - pm[0]) - (mp[0] - mm[0]);

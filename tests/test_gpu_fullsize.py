@@ -4,7 +4,7 @@ take too long: the 128^3 Hex8 brick (2,097,152 elements, 6,440,067 dofs).
 * the HVP is symmetric: v.(K w) = w.(K v)
 * the HVP is linear: K(a v + w) = a K v + K w
 * the quadratic energy is consistent with the HVP: E(u) = 1/2 u.(K u) (linear elasticity)
-* the FP32 box kernel agrees with the FP64 kernel at full size
+* the FP32 kernels (grid stencil; lattice and box element blocks) agree with FP64
 Tolerances: FP64 1e-12 relative; FP32 results against FP64 2e-5 relative (max-norm).
 """
 
@@ -54,11 +54,22 @@ def test_full_size_fp32_box_kernel_vs_fp64(brick):
     r64 = en.residual(1e-3 * v, fixed=brick["fixed"])
     r32 = en.residual((1e-3 * v).float(), fixed=brick["fixed"])
     assert _rel(r32.double(), r64) < 2e-5
-    # the no-staging box kernel (plan edge terms) and the staging one agree bit for bit
+    # the element-block kernels of the same plan (the brick runs the grid stencil by
+    # default): FP32 lattice / box kernel against FP64, and the no-staging box kernel
+    # (plan edge terms) bit for bit equal to the staging one
+    assert plan.grid
+    plan.grid = False
     saved = plan.struct.box_geom32
     try:
+        y32b = en.hvp(None, v.float())
+        assert _rel(y32b.double(), y64) < 2e-5
+        n_lat = plan.struct.n_lattice_blocks
+        plan.struct.n_lattice_blocks = 0
+        y32g = en.hvp(None, v.float())
         plan.struct.box_geom32 = None
         y32x = en.hvp(None, v.float())
+        plan.struct.n_lattice_blocks = n_lat
     finally:
         plan.struct.box_geom32 = saved
-    assert torch.equal(y32, y32x)
+        plan.grid = True
+    assert torch.equal(y32g, y32x)

@@ -269,3 +269,36 @@ def test_grid_detect_structured_bricks():
     assert not plan.grid and tuple(plan.struct.grid_nodes) == (0, 0, 0)
     plan.grid = True
     assert tuple(plan.struct.grid_nodes) == (8, 6, 7)
+
+
+def test_pattern_and_colors_bit_exact_at_kuhn96():
+    """The Neo-Hookean configuration's full size (Kuhn 96^3 Tet4, 2,738,019 dofs,
+    121,188,969 nonzeros): pattern and natural-order distance-2 colouring bit for bit
+    against the oracle's C restatement of _extraction.py:37-102 and
+    _coloring.py:27-48, 136-153 (the Python oracle's loops are too slow at this size;
+    the C restatement equals it on the small cases of this file)."""
+    from oracle import cbuild
+
+    c, e = om.kuhn_box((1, 1, 1), (96, 96, 96), origin=(0, 0, 0))
+    ip, ix = cbuild.pattern(e, c.shape[0], 3)
+    csr = sparse.pattern_from_mesh(Mesh(c, e, device="cpu"), 3)
+    assert ix.size == 121188969
+    assert np.array_equal(csr.indptr, ip) and np.array_equal(csr.indices, ix)
+    del csr
+    colors = cbuild.d2_colors(ip, ix)
+    got = sparse.distance2_colors(ip.astype(np.int32), ix, ip.size - 1)
+    assert int(colors.max()) + 1 == 90
+    assert np.array_equal(np.asarray(got), colors)
+
+
+@pytest.mark.parametrize("case", ["tri", "hex", "tet"])
+def test_c_oracle_equals_python_oracle(case):
+    from oracle import cbuild
+
+    c, e, nd = {"tri": om.unit_square(9, 7) + (1,), "hex": om.brick(3, 4, 2) + (3,),
+                "tet": om.kuhn_box((1, 1, 1), (4, 3, 5), origin=(0, 0, 0)) + (3,)}[case]
+    ip, ix = cbuild.pattern(e, c.shape[0], nd)
+    ref = osp.pattern_from_mesh(c, e, nd)
+    assert np.array_equal(ip, ref.indptr) and np.array_equal(ix, ref.indices)
+    assert np.array_equal(cbuild.d2_colors(ip, ix),
+                          osp.distance2_colors(ref.indptr, ref.indices, ref.shape[0]))

@@ -38,12 +38,25 @@
 // result is deterministic and needs no atomics, partial slots or second pass.
 #include <type_traits>
 
+#include "tg_cg.cuh"
 #include "tg_common.cuh"
 #include "tg_internal.h"
 
 namespace tg {
 
-constexpr int GR_TX = 32, GR_TY = 8, GR_THREADS = GR_TX * GR_TY;
+// Tile height (node rows per CTA), CTAs per SM asked of the register allocator (FP32;
+// FP64 asks for 2, its kernels being FP64-pipe bound), and interior planes per tile;
+// measured on GB300 (128^3 brick).
+#ifndef TG_GRID_TY
+#define TG_GRID_TY 8
+#endif
+#ifndef TG_GRID_MINB
+#define TG_GRID_MINB 3
+#endif
+#ifndef TG_GRID_TZ
+#define TG_GRID_TZ 16
+#endif
+constexpr int GR_TX = 32, GR_TY = TG_GRID_TY, GR_THREADS = GR_TX * GR_TY;
 constexpr int GR_PX = GR_TX + 2, GR_PY = GR_TY + 2, GR_PLANE = GR_PX * GR_PY;  // 340
 constexpr int GR_SLOTS = (GR_PLANE + GR_THREADS - 1) / GR_THREADS;            // 2
 
@@ -89,6 +102,86 @@ __device__ __forceinline__ T load_in(const T* __restrict__ in, const uint8_t* __
   T x = __ldg(in + dof);
   if (MASK && __ldg(fixed + dof)) x = T(0);
   return x;
+}
+
+// One input plane's contributions to the outputs below (accM, z - 1), at (accP, z) and
+// above (accN, z + 1) the plane, for the node column at shared-memory slot c0.
+//
+// Difference form (FP32): every block row of the stencil sums to zero (a rigid
+// translation has no stiffness), so each in-plane neighbour enters as its difference
+// to the column's value in that plane, and the column's own values enter as the
+// second difference along z with the in-plane row sum R1 of the |dz| = 1
+// coefficients.  For smooth fields this keeps the FP32 result as accurate as its
+// rounded input allows (the value form loses a factor of ~1/h^2 to cancellation).
+// FP64 uses the value form (fewer operations on the FP64 pipe, no precision to win).
+// prev: the column's value in the previous plane (difference form, updated here);
+// ctr: this plane's column value (out).
+template <class T>
+__device__ __forceinline__ void stencil_plane(const GridCoef<T>& P,
+                                              const typename Vec4<T>::type* buf, int c0,
+                                              T (&accM)[3], T (&accP)[3], T (&accN)[3],
+                                              T (&prev)[3], T (&ctr)[3]) {
+  using V4 = typename Vec4<T>::type;
+  constexpr bool DIFF = std::is_same<T, float>::value;
+  // the nine in-plane neighbours, v[dy + 1][dx + 1]
+  V4 v[3][3];
+#pragma unroll
+  for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+    for (int dx = 0; dx < 3; ++dx) v[dy][dx] = buf[c0 + (dx - 1) + GR_PX * (dy - 1)];
+  const T a0[3] = {v[1][1].x, v[1][1].y, v[1][1].z};
+  const T xm[3] = {v[1][0].x, v[1][0].y, v[1][0].z}, xp[3] = {v[1][2].x, v[1][2].y, v[1][2].z};
+  const T ym[3] = {v[0][1].x, v[0][1].y, v[0][1].z}, yp[3] = {v[2][1].x, v[2][1].y, v[2][1].z};
+  const T mm[3] = {v[0][0].x, v[0][0].y, v[0][0].z}, pm[3] = {v[0][2].x, v[0][2].y, v[0][2].z};
+  const T mp[3] = {v[2][0].x, v[2][0].y, v[2][0].z}, pp[3] = {v[2][2].x, v[2][2].y, v[2][2].z};
+  // diagonal blocks grouped by |dx|, |dy|
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ctr[a] = a0[a];
+    if constexpr (DIFF) {
+      const T gx = (xm[a] - a0[a]) + (xp[a] - a0[a]);
+      const T gy = (ym[a] - a0[a]) + (yp[a] - a0[a]);
+      const T gc = ((mm[a] - a0[a]) + (mp[a] - a0[a])) + ((pm[a] - a0[a]) + (pp[a] - a0[a]));
+      const T s0 = fma(P.c[a][3], gc, fma(P.c[a][2], gy, P.c[a][1] * gx));
+      const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, P.c[a][5] * gx));
+      const T dz = a0[a] - prev[a];
+      accP[a] = fma(-P.r1[a], dz, accP[a] + s0);
+      accM[a] = fma(P.r1[a], dz, accM[a] + s1);
+      accN[a] += s1;
+      prev[a] = a0[a];
+    } else {
+      const T gx = xm[a] + xp[a], gy = ym[a] + yp[a];
+      const T gc = (mm[a] + mp[a]) + (pm[a] + pp[a]);
+      accP[a] = fma(P.c[a][3], gc, fma(P.c[a][2], gy, fma(P.c[a][1], gx, fma(P.c[a][0], a0[a], accP[a]))));
+      const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, fma(P.c[a][5], gx, P.c[a][4] * a0[a])));
+      accM[a] += s1;
+      accN[a] += s1;
+    }
+  }
+  // x-y blocks: C = qxy(|dz|) dx dy, the cross sum of the in-plane corners
+  const T wx = (pp[0] - pm[0]) - (mp[0] - mm[0]);
+  const T wy = (pp[1] - pm[1]) - (mp[1] - mm[1]);
+  accP[0] = fma(P.qxy[0], wy, accP[0]);
+  accM[0] = fma(P.qxy[1], wy, accM[0]);
+  accN[0] = fma(P.qxy[1], wy, accN[0]);
+  accP[1] = fma(P.qxy[0], wx, accP[1]);
+  accM[1] = fma(P.qxy[1], wx, accM[1]);
+  accN[1] = fma(P.qxy[1], wx, accN[1]);
+  // x-z blocks: C = qxz(|dy|) dx dz: odd in x, summed over dy with M_y
+  const T uz_x = fma(P.qxz[1], ((pm[2] - mm[2]) + (pp[2] - mp[2])), P.qxz[0] * (xp[2] - xm[2]));
+  const T ux_x = fma(P.qxz[1], ((pm[0] - mm[0]) + (pp[0] - mp[0])), P.qxz[0] * (xp[0] - xm[0]));
+  // y-z blocks: C = qyz(|dx|) dy dz: odd in y, summed over dx with M_x
+  const T uz_y = fma(P.qyz[1], ((mp[2] - mm[2]) + (pp[2] - pm[2])), P.qyz[0] * (yp[2] - ym[2]));
+  const T uy_y = fma(P.qyz[1], ((mp[1] - mm[1]) + (pp[1] - pm[1])), P.qyz[0] * (yp[1] - ym[1]));
+  // dz = plane - output: the output below (z - 1) sees dz = +1, the one above -1
+  accM[0] += uz_x;
+  accN[0] -= uz_x;
+  accM[2] += ux_x;
+  accN[2] -= ux_x;
+  accM[1] += uz_y;
+  accN[1] -= uz_y;
+  accM[2] += uy_y;
+  accN[2] -= uy_y;
 }
 
 // Interior tile: thread (lx, ly) owns node column (x0 + lx, y0 + ly), planes
@@ -148,76 +241,8 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   for (int a = 0; a < 3; ++a) accM[a] = accP[a] = accN[a] = T(0);
   const int c0 = (lx + 1) + GR_PX * (ly + 1);
 
-  // Difference form (FP32): every block row of the stencil sums to zero (a rigid translation
-  // has no stiffness), so each in-plane neighbour enters as its difference to the
-  // column's value in that plane, and the column's own values enter as the second
-  // difference along z with the in-plane row sum R1 of the |dz| = 1 coefficients.
-  // For smooth fields this keeps the FP32 result as accurate as its rounded input
-  // allows (the value form loses a factor of ~1/h^2 to cancellation).
-  constexpr bool DIFF = std::is_same<T, float>::value;
-  T prev[3];  // the column's value in the previous plane (difference form)
-  auto plane_step = [&](const V4* buf) {
-    // the nine in-plane neighbours, v[dy + 1][dx + 1]
-    V4 v[3][3];
-#pragma unroll
-    for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-      for (int dx = 0; dx < 3; ++dx) v[dy][dx] = buf[c0 + (dx - 1) + GR_PX * (dy - 1)];
-    const T a0[3] = {v[1][1].x, v[1][1].y, v[1][1].z};
-    const T xm[3] = {v[1][0].x, v[1][0].y, v[1][0].z}, xp[3] = {v[1][2].x, v[1][2].y, v[1][2].z};
-    const T ym[3] = {v[0][1].x, v[0][1].y, v[0][1].z}, yp[3] = {v[2][1].x, v[2][1].y, v[2][1].z};
-    const T mm[3] = {v[0][0].x, v[0][0].y, v[0][0].z}, pm[3] = {v[0][2].x, v[0][2].y, v[0][2].z};
-    const T mp[3] = {v[2][0].x, v[2][0].y, v[2][0].z}, pp[3] = {v[2][2].x, v[2][2].y, v[2][2].z};
-    // diagonal blocks grouped by |dx|, |dy|: in FP32 as second differences (difference
-    // form), in FP64 from the values themselves (fewer operations on the FP64 pipe;
-    // no precision to win there)
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if constexpr (DIFF) {
-        const T gx = (xm[a] - a0[a]) + (xp[a] - a0[a]);
-        const T gy = (ym[a] - a0[a]) + (yp[a] - a0[a]);
-        const T gc = ((mm[a] - a0[a]) + (mp[a] - a0[a])) + ((pm[a] - a0[a]) + (pp[a] - a0[a]));
-        const T s0 = fma(P.c[a][3], gc, fma(P.c[a][2], gy, P.c[a][1] * gx));
-        const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, P.c[a][5] * gx));
-        const T dz = a0[a] - prev[a];
-        accP[a] = fma(-P.r1[a], dz, accP[a] + s0);
-        accM[a] = fma(P.r1[a], dz, accM[a] + s1);
-        accN[a] += s1;
-        prev[a] = a0[a];
-      } else {
-        const T gx = xm[a] + xp[a], gy = ym[a] + yp[a];
-        const T gc = (mm[a] + mp[a]) + (pm[a] + pp[a]);
-        accP[a] = fma(P.c[a][3], gc, fma(P.c[a][2], gy, fma(P.c[a][1], gx, fma(P.c[a][0], a0[a], accP[a]))));
-        const T s1 = fma(P.c[a][7], gc, fma(P.c[a][6], gy, fma(P.c[a][5], gx, P.c[a][4] * a0[a])));
-        accM[a] += s1;
-        accN[a] += s1;
-      }
-    }
-    // x-y blocks: C = qxy(|dz|) dx dy, the cross sum of the in-plane corners
-    const T wx = (pp[0] - pm[0]) - (mp[0] - mm[0]);
-    const T wy = (pp[1] - pm[1]) - (mp[1] - mm[1]);
-    accP[0] = fma(P.qxy[0], wy, accP[0]);
-    accM[0] = fma(P.qxy[1], wy, accM[0]);
-    accN[0] = fma(P.qxy[1], wy, accN[0]);
-    accP[1] = fma(P.qxy[0], wx, accP[1]);
-    accM[1] = fma(P.qxy[1], wx, accM[1]);
-    accN[1] = fma(P.qxy[1], wx, accN[1]);
-    // x-z blocks: C = qxz(|dy|) dx dz: odd in x, summed over dy with M_y
-    const T uz_x = fma(P.qxz[1], ((pm[2] - mm[2]) + (pp[2] - mp[2])), P.qxz[0] * (xp[2] - xm[2]));
-    const T ux_x = fma(P.qxz[1], ((pm[0] - mm[0]) + (pp[0] - mp[0])), P.qxz[0] * (xp[0] - xm[0]));
-    // y-z blocks: C = qyz(|dx|) dy dz: odd in y, summed over dx with M_x
-    const T uz_y = fma(P.qyz[1], ((mp[2] - mm[2]) + (pp[2] - pm[2])), P.qyz[0] * (yp[2] - ym[2]));
-    const T uy_y = fma(P.qyz[1], ((mp[1] - mm[1]) + (pp[1] - pm[1])), P.qyz[0] * (yp[1] - ym[1]));
-    // dz = plane - output: the output below (z - 1) sees dz = +1, the one above -1
-    accM[0] += uz_x;
-    accN[0] -= uz_x;
-    accM[2] += ux_x;
-    accN[2] -= ux_x;
-    accM[1] += uz_y;
-    accN[1] -= uz_y;
-    accM[2] += uy_y;
-    accN[2] -= uy_y;
-  };
+  T prev[3], ctr[3];  // the column's value in the previous / current plane
+  auto plane_step = [&](const V4* buf) { stencil_plane<T>(P, buf, c0, accM, accP, accN, prev, ctr); };
 
   auto emit = [&](int z, const T (&acc)[3]) {
     if (!own || z < zs || z >= ze) return;
@@ -340,7 +365,7 @@ __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restr
 }
 
 template <class T, int MODE, bool MASK>
-__global__ void __launch_bounds__(GR_THREADS)
+__global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
     grid_le_kernel(const __grid_constant__ GridCoef<T> P, const T* __restrict__ in,
                    const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
                    T* __restrict__ y) {
@@ -353,6 +378,228 @@ __global__ void __launch_bounds__(GR_THREADS)
                                  reinterpret_cast<T*>(sm));
   } else {
     grid_interior<T, MODE, MASK>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm);
+  }
+}
+
+// ------------------------------------------------------------------- fused CG step
+// One Jacobi-CG iteration's search direction and operator product in one pass:
+//   p = dinv r + beta p_old   (beta from the previous update; 0 after a restart)
+//   q = A p                   (the masked operator: fixed inputs read as 0, q = p there)
+//   alpha = rz / (p . q)      (the CTA that arrives last adds the CTAs' partials in
+//                              index order and stores alpha in the device scalars)
+// Every CTA stages p at its halo nodes itself (from r, dinv, p_old; the same bits as the
+// owner's), and each node's p and q are written once, by the thread that owns the node.
+// p_old and p must be different buffers (neighbouring CTAs still read p_old).
+template <class T>
+struct CgStep {
+  const T* r;
+  const T* dinv;
+  const T* pold;
+  T* pnew;
+  T* q;
+  const uint8_t* fixed;
+  double* scal;
+  double* part;
+  unsigned* ticket;
+};
+
+template <class T, bool MASK>
+__device__ void grid_cg_interior(const GridCoef<T>& P, int item, const CgStep<T>& A, T beta,
+                                 DotAcc<T>& dot, typename Vec4<T>::type* sm) {
+  using V4 = typename Vec4<T>::type;
+  const int tid = threadIdx.x;
+  const int nx = P.nx, ny = P.ny, nz = P.nz;
+  const int tx = item % P.tiles_x;
+  const int rest = item / P.tiles_x;
+  const int ty = rest % P.tiles_y;
+  const int tzi = rest / P.tiles_y;
+  const int x0 = 1 + tx * GR_TX, y0 = 1 + ty * GR_TY;
+  const int zs = 1 + tzi * P.tz;
+  const int ze = min(zs + P.tz, nz - 1);
+  const int lx = tid % GR_TX, ly = tid / GR_TX;
+  const int x = x0 + lx, yy = y0 + ly;
+  const bool own = (x <= nx - 2) && (yy <= ny - 2);
+  const int64_t plane_nodes = (int64_t)nx * ny;
+
+  int64_t soff[GR_SLOTS];  // node offset within a plane, -1: outside the grid / no slot
+  bool sown[GR_SLOTS];     // the slot's node is an output node of this tile (x, y)
+#pragma unroll
+  for (int k = 0; k < GR_SLOTS; ++k) {
+    const int s = tid + k * GR_THREADS;
+    soff[k] = -1;
+    sown[k] = false;
+    if (s < GR_PLANE) {
+      const int hx = s % GR_PX, hy = s / GR_PX;
+      const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+      if (gx < nx && gy < ny) soff[k] = gx + (int64_t)nx * gy;
+      sown[k] = hx >= 1 && hx <= GR_TX && hy >= 1 && hy <= GR_TY && gx <= nx - 2 && gy <= ny - 2;
+    }
+  }
+  // one plane ahead in registers: r, dinv, p_old and the mask bits of the staged slots
+  T rr[GR_SLOTS][3], dd[GR_SLOTS][3], po[GR_SLOTS][3];
+  int fb[GR_SLOTS];
+  auto load_plane = [&](int p) {
+#pragma unroll
+    for (int k = 0; k < GR_SLOTS; ++k) {
+      fb[k] = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) rr[k][d] = dd[k][d] = po[k][d] = T(0);
+      if (soff[k] >= 0 && p <= ze) {
+        const int64_t base = 3 * (soff[k] + plane_nodes * p);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          rr[k][d] = __ldg(A.r + base + d);
+          dd[k][d] = __ldg(A.dinv + base + d);
+          po[k][d] = __ldg(A.pold + base + d);
+          if (MASK && __ldg(A.fixed + base + d)) fb[k] |= 1 << d;
+        }
+      }
+    }
+  };
+  auto store_plane = [&](V4* buf, int p) {
+    const bool out_plane = p >= zs && p < ze;
+#pragma unroll
+    for (int k = 0; k < GR_SLOTS; ++k) {
+      const int s = tid + k * GR_THREADS;
+      if (s < GR_PLANE) {
+        T pn[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) pn[d] = fma(beta, po[k][d], rr[k][d] * dd[k][d]);
+        if (sown[k] && out_plane) {
+          const int64_t base = 3 * (soff[k] + plane_nodes * p);
+#pragma unroll
+          for (int d = 0; d < 3; ++d) A.pnew[base + d] = pn[d];
+        }
+        buf[s] = make4<T>((fb[k] & 1) ? T(0) : pn[0], (fb[k] & 2) ? T(0) : pn[1],
+                          (fb[k] & 4) ? T(0) : pn[2]);
+      }
+    }
+  };
+
+  T accM[3], accP[3], accN[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) accM[a] = accP[a] = accN[a] = T(0);
+  const int c0 = (lx + 1) + GR_PX * (ly + 1);
+  T prev[3], ctr[3] = {T(0), T(0), T(0)};
+
+  auto emit = [&](int z, const T (&acc)[3], const T (&pc)[3]) {
+    if (!own || z < zs || z >= ze) return;
+    const int64_t base = 3 * (x + (int64_t)nx * yy + plane_nodes * z);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      T pv = pc[d], qv = acc[d];
+      if (MASK && __ldg(A.fixed + base + d)) {
+        pv = __ldcg(A.pnew + base + d);  // written by this CTA's staging, before a barrier
+        qv = pv;
+      }
+      A.q[base + d] = qv;
+      dot.add(pv, qv);
+    }
+  };
+
+  V4* buf0 = sm;
+  V4* buf1 = sm + GR_PLANE;
+  load_plane(zs - 1);
+  store_plane(buf0, zs - 1);
+  load_plane(zs);
+  __syncthreads();
+  {
+    const V4 c = buf0[c0];
+    prev[0] = c.x;
+    prev[1] = c.y;
+    prev[2] = c.z;
+  }
+  for (int p = zs - 1; p <= ze; ++p) {
+    const bool even = ((p - zs + 1) & 1) == 0;
+    V4* cur = even ? buf0 : buf1;
+    V4* nxt = even ? buf1 : buf0;
+    const T pc[3] = {ctr[0], ctr[1], ctr[2]};
+    stencil_plane<T>(P, cur, c0, accM, accP, accN, prev, ctr);
+    emit(p - 1, accM, pc);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      accM[a] = accP[a];
+      accP[a] = accN[a];
+      accN[a] = T(0);
+    }
+    if (p + 1 <= ze) store_plane(nxt, p + 1);
+    load_plane(p + 2);
+    __syncthreads();
+  }
+}
+
+template <class T, bool MASK>
+__device__ void grid_cg_boundary(const GridCoef<T>& P, int64_t t0, const CgStep<T>& A, T beta,
+                                 DotAcc<T>& dot, T* ke) {
+  for (int i = threadIdx.x; i < 8 * 8 * 9; i += blockDim.x) ke[i] = (&P.ke[0][0][0][0])[i];
+  __syncthreads();
+  const int64_t t = t0 + threadIdx.x;
+  if (t >= P.n_boundary) return;
+  const int nx = P.nx, ny = P.ny, nz = P.nz;
+  int x, yy, z;
+  boundary_node(t, nx, ny, nz, x, yy, z);
+  auto pval = [&](int64_t dof) {
+    return fma(beta, __ldg(A.pold + dof), __ldg(A.r + dof) * __ldg(A.dinv + dof));
+  };
+  T acc[3] = {T(0), T(0), T(0)};
+  for (int o = 0; o < 8; ++o) {
+    const int ox = o & 1, oy = (o >> 1) & 1, oz = o >> 2;
+    const int cx = x - ox, cy = yy - oy, cz = z - oz;
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= nx - 1 || cy >= ny - 1 || cz >= nz - 1) continue;
+    const T* kr = ke + o * 72;
+#pragma unroll
+    for (int cm = 0; cm < 8; ++cm) {
+      const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
+                                                         (int64_t)ny * (cz + (cm >> 2)));
+      T v[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        v[d] = pval(3 * g + d);
+        if (MASK && __ldg(A.fixed + 3 * g + d)) v[d] = T(0);
+      }
+      const T* k9 = kr + cm * 9;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a] = fma(k9[3 * a + 2], v[2], fma(k9[3 * a + 1], v[1], fma(k9[3 * a], v[0], acc[a])));
+    }
+  }
+  const int64_t base = 3 * (x + (int64_t)nx * (yy + (int64_t)ny * z));
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const T pv = pval(base + d);
+    T qv = acc[d];
+    if (MASK && __ldg(A.fixed + base + d)) qv = pv;
+    A.pnew[base + d] = pv;
+    A.q[base + d] = qv;
+    dot.add(pv, qv);
+  }
+}
+
+template <class T, bool MASK>
+__global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
+    grid_cg_kernel(const __grid_constant__ GridCoef<T> P, const __grid_constant__ CgStep<T> A) {
+  using V4 = typename Vec4<T>::type;
+  __shared__ V4 sm[2 * GR_PLANE];
+  const T beta = (T)A.scal[SCAL_BETA];
+  DotAcc<T> dot;
+  const int b = blockIdx.x;
+  if (b < P.n_boundary_ctas) {
+    grid_cg_boundary<T, MASK>(P, (int64_t)b * GR_THREADS, A, beta, dot, reinterpret_cast<T*>(sm));
+  } else {
+    grid_cg_interior<T, MASK>(P, b - P.n_boundary_ctas, A, beta, dot, sm);
+  }
+  double v[1] = {dot.value()};
+  block_reduce_store<1, GR_THREADS>(v, A.part + blockIdx.x);
+  if (!last_cta(A.ticket)) return;
+  double w[1] = {0.0};
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += GR_THREADS) w[0] += __ldcg(A.part + i);
+  __shared__ double out[1];
+  block_reduce_store<1, GR_THREADS>(w, out);
+  if (threadIdx.x == 0) {
+    const double pq = out[0];
+    A.scal[SCAL_PQ] = pq;
+    const bool bad = !(pq > 0.0) || !isfinite(pq) || A.scal[SCAL_FLAG] != 0.0;
+    if (bad) A.scal[SCAL_FLAG] = 1.0;
+    A.scal[SCAL_ALPHA] = bad ? 0.0 : A.scal[SCAL_RZ] / pq;
   }
 }
 
@@ -420,31 +667,39 @@ static void grid_coefficients(const double h[3], double mu, double lam, GridCoef
     }
 }
 
+// Coefficients and tiling of a structured-brick plan; returns the launch's CTA count
+// (boundary CTAs first, then the interior tiles), or -1 when it does not fit an int.
 template <class T>
-static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, const T* v,
-                            const uint8_t* fixed, T* y, double mu, double lam,
-                            cudaStream_t st) {
-  GridCoef<T> P;
+static int64_t grid_setup(const tg_block_plan* plan, double mu, double lam, GridCoef<T>& P) {
   const int nx = plan->grid_nodes[0], ny = plan->grid_nodes[1], nz = plan->grid_nodes[2];
   grid_coefficients<T>(plan->grid_h, mu, lam, P);
   P.nx = nx;
   P.ny = ny;
   P.nz = nz;
-  // interior planes per tile: about four tiles per resident CTA slot over the grid
   const int ix = nx - 2, iy = ny - 2, iz = nz - 2;
   P.tiles_x = ix > 0 ? (ix + GR_TX - 1) / GR_TX : 0;
   P.tiles_y = iy > 0 ? (iy + GR_TY - 1) / GR_TY : 0;
-  P.tz = 16;
+  P.tz = TG_GRID_TZ;
   P.tiles_z = iz > 0 ? (iz + P.tz - 1) / P.tz : 0;
   const int64_t n_int = (int64_t)P.tiles_x * P.tiles_y * P.tiles_z;
   P.n_boundary = (int64_t)nx * ny * nz - (int64_t)(ix > 0 ? ix : 0) * (iy > 0 ? iy : 0) *
                                              (iz > 0 ? iz : 0);
   const int64_t n_bnd_ctas = (P.n_boundary + GR_THREADS - 1) / GR_THREADS;
-  if (n_int + n_bnd_ctas > 0x7fffffff) return set_error(TG_ERR_VALUE, "grid too large");
+  if (n_int + n_bnd_ctas > 0x7fffffff) return -1;
   P.n_boundary_ctas = (int)n_bnd_ctas;
+  return n_int + n_bnd_ctas;
+}
+
+template <class T>
+static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, const T* v,
+                            const uint8_t* fixed, T* y, double mu, double lam,
+                            cudaStream_t st) {
+  GridCoef<T> P;
+  const int64_t n = grid_setup<T>(plan, mu, lam, P);
+  if (n < 0) return set_error(TG_ERR_VALUE, "grid too large");
+  if (n == 0) return TG_OK;
   const T* in = (mode == TG_MODE_HVP) ? v : u;
-  const unsigned grid = (unsigned)(n_int + n_bnd_ctas);
-  if (grid == 0) return TG_OK;
+  const unsigned grid = (unsigned)n;
   if (mode == TG_MODE_HVP) {
     if (fixed)
       grid_le_kernel<T, TG_MODE_HVP, true><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
@@ -454,6 +709,31 @@ static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, con
     grid_le_kernel<T, TG_MODE_RESIDUAL, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
   }
   return launch_check("grid linear-elastic kernel");
+}
+
+int64_t grid_cg_ctas(const tg_block_plan* plan) {
+  GridCoef<float> P;
+  return grid_setup<float>(plan, 1.0, 1.0, P);
+}
+
+int launch_grid_cg(const tg_block_plan* plan, int prec, double mu, double lam, const void* r,
+                   const void* dinv, const void* pold, void* pnew, void* q,
+                   const uint8_t* fixed, double* scal, double* part, unsigned* ticket,
+                   cudaStream_t st) {
+  auto go = [&](auto t) -> int {
+    using T = decltype(t);
+    GridCoef<T> P;
+    const int64_t n = grid_setup<T>(plan, mu, lam, P);
+    if (n <= 0) return set_error(TG_ERR_VALUE, "grid CG: empty or too large grid");
+    CgStep<T> A{(const T*)r, (const T*)dinv, (const T*)pold, (T*)pnew, (T*)q, fixed, scal, part,
+                ticket};
+    if (fixed)
+      grid_cg_kernel<T, true><<<(unsigned)n, GR_THREADS, 0, st>>>(P, A);
+    else
+      grid_cg_kernel<T, false><<<(unsigned)n, GR_THREADS, 0, st>>>(P, A);
+    return launch_check("grid CG step");
+  };
+  return prec == TG_F32 ? go(0.f) : go(0.0);
 }
 
 int launch_grid_le(const tg_block_plan* plan, int prec, int mode, const void* u, const void* v,

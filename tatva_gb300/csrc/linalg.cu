@@ -14,90 +14,12 @@
 #include <cmath>
 #include <vector>
 
+#include "tg_cg.cuh"
 #include "tg_common.cuh"
 #include "tg_dispatch.cuh"
+#include "tg_internal.h"
 
 namespace tg {
-
-constexpr int DOT_CHUNKS = 2048;
-constexpr int DOT_THREADS = 256;
-constexpr int SCAL_RZ = 0, SCAL_PQ = 1, SCAL_ALPHA = 2, SCAL_BETA = 3, SCAL_RR = 4,
-              SCAL_FLAG = 6, SCAL_N = 8;
-
-// ------------------------------------------------------------------ dot accumulators
-// FP32 vectors: each thread accumulates x_i y_i as an unevaluated pair (hi, lo) of
-// floats -- the product is split exactly with an FMA and added with a two-sum, so the
-// thread's partial keeps about 48 bits -- and only the per-thread partials enter the
-// FP64 tree reduction.  (This GPU's FP64 rate is a small fraction of FP32: per-element
-// FP64 conversions and multiply-adds made the dots several times slower than their
-// memory traffic.)  FP64 vectors accumulate in FP64.
-template <class T>
-struct DotAcc;
-template <>
-struct DotAcc<float> {
-  float hi = 0.f, lo = 0.f;
-  __device__ __forceinline__ void add(float a, float b) {
-    const float pr = a * b;
-    const float pe = fmaf(a, b, -pr);
-    const float s = hi + pr;
-    const float bp = s - hi;
-    const float err = (hi - (s - bp)) + (pr - bp);
-    hi = s;
-    lo += err + pe;
-  }
-  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
-template <>
-struct DotAcc<double> {
-  double v = 0.0;
-  __device__ __forceinline__ void add(double a, double b) { v += a * b; }
-  __device__ __forceinline__ double value() const { return v; }
-};
-
-// ------------------------------------------------------------------ reductions
-// Sum of one value per thread of the CTA into out[k] (thread 0 writes): a fixed tree
-// (shuffles inside each warp, then the warps' sums in warp order), so the result does
-// not depend on timing.  Ends with a barrier: the CTA may call it again.
-template <int K>
-__device__ __forceinline__ void block_reduce_store(double (&v)[K], double* __restrict__ out) {
-  constexpr int NW = DOT_THREADS / 32;
-  __shared__ double sh[K][NW];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-    if (lane == 0) sh[k][warp] = v[k];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double a = sh[k][0];
-#pragma unroll
-      for (int w = 1; w < NW; ++w) a += sh[k][w];
-      out[k] = a;
-    }
-  }
-  __syncthreads();
-}
-
-// Called by every thread after thread 0 stored this CTA's partials: true in the CTA
-// that arrives last, which then sees every CTA's partials (read them with __ldcg).
-// That CTA resets the ticket for the next launch.  An arrival counter, no waiting.
-__device__ __forceinline__ bool last_cta(unsigned* ticket) {
-  __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned t = atomicAdd(ticket, 1u);
-    last = (t == gridDim.x - 1);
-    if (last) *ticket = 0u;
-  }
-  __syncthreads();
-  if (last) __threadfence();
-  return last;
-}
 
 // Chunk count of the fixed partition of an n-vector: one chunk per 8192 entries, at
 // most DOT_CHUNKS (about five CTAs per SM for the largest vectors here, one wave; the
@@ -358,6 +280,7 @@ __global__ void cg_init_final_kernel(const double* __restrict__ part, double* __
     scal[SCAL_RZ] = out[0];
     scal[SCAL_RR] = out[1];
     scal[SCAL_FLAG] = 0.0;
+    scal[SCAL_BETA] = 0.0;  // the fused grid step rebuilds p = dinv r + 0 p_old
   }
 }
 
@@ -674,17 +597,37 @@ namespace tg {
 
 struct CgBuffers {
   void *r, *p, *q, *dinv, *apply_ws;
+  void* p2;    // second search-direction buffer of the fused grid step (ping-pong)
+  int parity;  // the current direction is (parity ? p2 : p)
+  bool grid;   // fused grid step (structured-brick linear elasticity)
   double *part, *scal;
   unsigned* ticket;  // [2] last-CTA arrival counters of the p.q and update kernels
   size_t apply_bytes;
+  void* pcur() const { return parity ? p2 : p; }
+  void* pnext() const { return parity ? p : p2; }
 };
+
+// The operator is linear elasticity on a structured brick whose plan carries the grid:
+// CG iterations use the fused grid step.
+static bool grid_op(const tg_operator_desc* op) {
+  return !op->csr_data && op->plan && op->elem == TG_HEX8 && op->mat.kind == TG_LINEAR_ELASTIC &&
+         op->mat.elem_param == nullptr && op->plan->grid_nodes[0] > 0 &&
+         (int64_t)op->plan->grid_nodes[0] * op->plan->grid_nodes[1] * op->plan->grid_nodes[2] ==
+             op->n_nodes &&
+         grid_cg_ctas(op->plan) > 0;
+}
+
+static int64_t cg_part_doubles(const tg_operator_desc* op) {
+  const int64_t g = grid_op(op) ? grid_cg_ctas(op->plan) : 0;
+  return g > 2 * DOT_CHUNKS ? g : 2 * DOT_CHUNKS;
+}
 
 static size_t cg_bytes(const tg_operator_desc* op) {
   const int64_t n = op_ndofs(op);
   const size_t vs = align256((size_t)n * prec_size(op->prec));
-  return 4 * vs + align256(tg_operator_workspace_bytes(op)) +
-         align256(DOT_CHUNKS * 2 * sizeof(double)) + align256(SCAL_N * sizeof(double)) +
-         align256(2 * sizeof(unsigned));
+  return (grid_op(op) ? 5 : 4) * vs + align256(tg_operator_workspace_bytes(op)) +
+         align256((size_t)cg_part_doubles(op) * sizeof(double)) +
+         align256(SCAL_N * sizeof(double)) + align256(2 * sizeof(unsigned));
 }
 
 static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
@@ -692,13 +635,16 @@ static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
   const int64_t n = op_ndofs(op);
   CgBuffers b;
   const size_t vb = (size_t)n * prec_size(op->prec);
+  b.grid = grid_op(op);
+  b.parity = 0;
   b.r = c.take(vb);
   b.p = c.take(vb);
   b.dinv = c.take(vb);
   b.q = c.take(vb);
+  b.p2 = b.grid ? c.take(vb) : nullptr;
   b.apply_bytes = tg_operator_workspace_bytes(op);
   b.apply_ws = c.take(b.apply_bytes);
-  b.part = (double*)c.take(DOT_CHUNKS * 2 * sizeof(double));
+  b.part = (double*)c.take((size_t)cg_part_doubles(op) * sizeof(double));
   b.scal = (double*)c.take(SCAL_N * sizeof(double));
   b.ticket = (unsigned*)c.take(2 * sizeof(unsigned));
   return b;
@@ -713,7 +659,7 @@ static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* 
   axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
   inv_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, diag, (T*)B.dinv);
   cg_init_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, (const T*)B.r, (const T*)B.dinv,
-                                                        (T*)B.p, B.part);
+                                                        (T*)B.pcur(), B.part);
   cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
   TG_TRY(cuda_check(cudaMemsetAsync(B.ticket, 0, 2 * sizeof(unsigned), st), "cg: counters"));
   return launch_check("cg restart");
@@ -723,6 +669,16 @@ template <class T>
 static int cg_iteration(const tg_operator_desc* op, T* x, const T* diag, CgBuffers& B,
                         cudaStream_t st) {
   const int64_t n = op_ndofs(op);
+  if (B.grid) {
+    // fused: p = dinv r + beta p_old, q = A p, alpha (one kernel); then the update
+    TG_TRY(launch_grid_cg(op->plan, op->prec, op->mat.p0, op->mat.p1, B.r, B.dinv, B.pcur(),
+                          B.pnext(), B.q, op->fixed, B.scal, B.part, B.ticket, st));
+    B.parity ^= 1;
+    cg_update_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(
+        n, B.scal, x, (T*)B.r, (const T*)B.pcur(), (const T*)B.q, (const T*)B.dinv, B.part,
+        B.ticket + 1);
+    return launch_check("cg iteration (grid)");
+  }
   TG_TRY(tg_operator_apply(op, B.p, B.q, B.apply_ws, B.apply_bytes, st));
   cg_pq_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n, B.part,
                                                       B.scal, B.ticket);
@@ -758,7 +714,9 @@ static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag
   int rc = TG_OK;
   while (*iters < max_iter) {
     const int k = (max_iter - *iters) < check_every ? (max_iter - *iters) : check_every;
-    if (can_capture && k == check_every) {
+    // a captured run must leave the direction buffers' parity as it found it (the fused
+    // grid step alternates them): graphs of an even number of iterations only
+    if (can_capture && k == check_every && (!B.grid || k % 2 == 0)) {
       if (!exec || graph_len != k) {
         cudaGraph_t graph;
         rc = cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cg: capture");

@@ -110,3 +110,38 @@ def test_grid_brick_128_properties(cuda):
     assert abs(s1 - s2) <= 1e-12 * (abs(s1) + abs(s2))
     assert rel(en.hvp(None, 2.0 * v - 3.0 * w), 2.0 * kv - 3.0 * kw) < 1e-13
     assert rel(en.hvp(None, v.float()), kv) < F32_TOL
+
+
+@pytest.mark.parametrize("check_every", [10, 7])
+def test_grid_cg_matches_element_cg_and_is_deterministic(cuda, check_every):
+    """The fused grid CG step (p update, HVP and p.q in one kernel) against the CG on
+    the element-block HVP: same tolerance reached, same solution to 1e-8; FP64 and
+    mixed precision; repeated solves bitwise equal (odd check_every: no graph)."""
+    from tatva_gb300 import solvers
+
+    c, e = om.brick(20, 12, 10, lengths=(2.0, 1.2, 1.0))
+    op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    en = materials.LinearElastic.from_young(op, 1.0, 0.3)
+    plan = en.plan()
+    assert plan.grid
+    fixed = np.zeros(en.n_dofs, np.uint8)
+    fixed.reshape(-1, 3)[c[:, 0] == 0.0] = 1
+    fixed = torch.as_tensor(fixed, device=cuda)
+    b = torch.zeros(en.n_dofs, dtype=torch.float64, device=cuda)
+    b.view(-1, 3)[torch.as_tensor(c[:, 0] == 2.0, device=cuda), 0] = 1e-3
+    r1 = solvers.cg(en, b, fixed=fixed, rtol=1e-10, check_every=check_every)
+    r2 = solvers.cg(en, b, fixed=fixed, rtol=1e-10, check_every=check_every)
+    m1 = solvers.mixed_cg(en, b, fixed=fixed, rtol=1e-10, check_every=check_every)
+    m2 = solvers.mixed_cg(en, b, fixed=fixed, rtol=1e-10, check_every=check_every)
+    assert r1.converged and m1.converged and r1.rel_res <= 1e-10 and m1.rel_res <= 1e-10
+    assert torch.equal(r1.x, r2.x) and torch.equal(m1.x, m2.x)
+    plan.grid = False
+    try:
+        e1 = solvers.cg(en, b, fixed=fixed, rtol=1e-10, check_every=check_every)
+        em = solvers.mixed_cg(en, b, fixed=fixed, rtol=1e-10, check_every=check_every)
+    finally:
+        plan.grid = True
+    assert e1.converged and em.converged
+    ref = e1.x.cpu().numpy()
+    for res in (r1, m1, em):
+        assert rel(res.x, ref) < 1e-8

@@ -442,11 +442,11 @@ def run_ours(args):
     conv = all(rr.converged and rr.rel_res <= RTOL for rr in results)
     inner = results[-1].iterations
     outer = results[-1].outer
-    # launches per mixed solve: per inner iteration 2 kernels on a structured brick (the
-    # fused direction + HVP + p.q step, the update), else the HVP plus 3 CG kernels; per
+    # launches per mixed solve: per inner iteration 3 kernels on a structured brick (the
+    # HVP with p.q, the update, the direction), else the HVP plus 3 CG kernels; per
     # refinement the FP64 HVP, 3 residual/norm kernels, the scale-down and the CG restart
     # (HVP + 4 kernels) and the update; 3 set-up kernels, and the Jacobi diagonal
-    per_inner = 2 if plan.grid else hvp_launches + 3
+    per_inner = 3 if plan.grid else hvp_launches + 3
     launches_per_solve = (inner * per_inner + (outer + 1) * (hvp_launches + 3)
                           + outer * (hvp_launches + 6) + 3 + hvp_launches)
 

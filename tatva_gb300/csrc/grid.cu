@@ -186,10 +186,10 @@ __device__ __forceinline__ void stencil_plane(const GridCoef<T>& P,
 
 // Interior tile: thread (lx, ly) owns node column (x0 + lx, y0 + ly), planes
 // [zs, ze) of output.
-template <class T, int MODE, bool MASK>
+template <class T, int MODE, bool MASK, bool DOT>
 __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restrict__ in,
                               const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
-                              T* __restrict__ y, typename Vec4<T>::type* sm) {
+                              T* __restrict__ y, typename Vec4<T>::type* sm, DotAcc<T>& dot) {
   using V4 = typename Vec4<T>::type;
   const int tid = threadIdx.x;
   const int nx = P.nx, ny = P.ny, nz = P.nz;
@@ -244,14 +244,21 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   T prev[3], ctr[3];  // the column's value in the previous / current plane
   auto plane_step = [&](const V4* buf) { stencil_plane<T>(P, buf, c0, accM, accP, accN, prev, ctr); };
 
-  auto emit = [&](int z, const T (&acc)[3]) {
+  // pc: the node's own input (the column's value in the output plane, masked): with
+  // DOT the product input . output of the owned dofs (fixed dofs: their unmasked input,
+  // which is also their output) enters the CTA's dot partial
+  auto emit = [&](int z, const T (&acc)[3], const T (&pc)[3]) {
     if (!own || z < zs || z >= ze) return;
     const int64_t base = 3 * (x + (int64_t)nx * yy + plane_nodes * z);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      T val = acc[d];
-      if (fixed && __ldg(fixed + base + d)) val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
+      T val = acc[d], pv = pc[d];
+      if (fixed && __ldg(fixed + base + d)) {
+        val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
+        pv = val;
+      }
       y[base + d] = val;
+      if constexpr (DOT) dot.add(pv, val);
     }
   };
 
@@ -271,9 +278,11 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
     prev[2] = c.z;
   }
   // planes p = zs - 1 .. ze, two per trip: buf0 holds p, buf1 gets p + 1
+  ctr[0] = ctr[1] = ctr[2] = T(0);
   for (int p = zs - 1; p <= ze; p += 2) {
+    T pc[3] = {ctr[0], ctr[1], ctr[2]};
     plane_step(buf0);
-    emit(p - 1, accM);
+    emit(p - 1, accM, pc);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       accM[a] = accP[a];
@@ -284,8 +293,10 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
     load_plane(p + 3, rB);
     __syncthreads();
     if (p + 1 > ze) break;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pc[a] = ctr[a];
     plane_step(buf1);
-    emit(p, accM);
+    emit(p, accM, pc);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       accM[a] = accP[a];
@@ -326,10 +337,10 @@ __device__ __forceinline__ void boundary_node(int64_t t, int nx, int ny, int nz,
   z = 1 + (int)(r / (ny - 2));
 }
 
-template <class T, int MODE, bool MASK>
+template <class T, int MODE, bool MASK, bool DOT>
 __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restrict__ in,
                               const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
-                              T* __restrict__ y, T* ke) {
+                              T* __restrict__ y, T* ke, DotAcc<T>& dot) {
   for (int i = threadIdx.x; i < 8 * 8 * 9; i += blockDim.x) ke[i] = (&P.ke[0][0][0][0])[i];
   __syncthreads();
   const int64_t t = t0 + threadIdx.x;
@@ -359,247 +370,59 @@ __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restr
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     T val = acc[d];
-    if (fixed && __ldg(fixed + base + d)) val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
+    T pv = T(0);
+    if constexpr (DOT) pv = __ldg(in + base + d);
+    if (fixed && __ldg(fixed + base + d)) {
+      val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
+      pv = val;
+    }
     y[base + d] = val;
+    if constexpr (DOT) dot.add(pv, val);
   }
 }
 
-template <class T, int MODE, bool MASK>
+// Device scalars and partials of the CG dot that a DOT launch produces.
+struct GridDot {
+  double* scal;    // SCAL_* slots: reads RZ and FLAG, writes PQ, ALPHA, FLAG
+  double* part;    // one partial per CTA
+  unsigned* ticket;  // zeroed arrival counter (reset by the last CTA)
+};
+
+// DOT: the launch also forms p.q of its input p and output q (every dof: the HVP's
+// fixed rows are the identity, so they add p^2) -- per CTA in a fixed order, the CTAs'
+// partials added by the CTA that arrives last in index order -- and stores
+// alpha = rz / (p.q) for the CG update (breakdown flag when p.q <= 0 or not finite).
+template <class T, int MODE, bool MASK, bool DOT>
 __global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
     grid_le_kernel(const __grid_constant__ GridCoef<T> P, const T* __restrict__ in,
                    const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
-                   T* __restrict__ y) {
+                   T* __restrict__ y, const GridDot D) {
   using V4 = typename Vec4<T>::type;
   __shared__ V4 sm[2 * GR_PLANE];
+  DotAcc<T> dot;
   // boundary CTAs first: they start with the first wave and overlap the interior tiles
   const int b = blockIdx.x;
   if (b < P.n_boundary_ctas) {
-    grid_boundary<T, MODE, MASK>(P, (int64_t)b * GR_THREADS, in, vin, fixed, y,
-                                 reinterpret_cast<T*>(sm));
+    grid_boundary<T, MODE, MASK, DOT>(P, (int64_t)b * GR_THREADS, in, vin, fixed, y,
+                                      reinterpret_cast<T*>(sm), dot);
   } else {
-    grid_interior<T, MODE, MASK>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm);
+    grid_interior<T, MODE, MASK, DOT>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm, dot);
   }
-}
-
-// ------------------------------------------------------------------- fused CG step
-// One Jacobi-CG iteration's search direction and operator product in one pass:
-//   p = dinv r + beta p_old   (beta from the previous update; 0 after a restart)
-//   q = A p                   (the masked operator: fixed inputs read as 0, q = p there)
-//   alpha = rz / (p . q)      (the CTA that arrives last adds the CTAs' partials in
-//                              index order and stores alpha in the device scalars)
-// Every CTA stages p at its halo nodes itself (from r, dinv, p_old; the same bits as the
-// owner's), and each node's p and q are written once, by the thread that owns the node.
-// p_old and p must be different buffers (neighbouring CTAs still read p_old).
-template <class T>
-struct CgStep {
-  const T* r;
-  const T* dinv;
-  const T* pold;
-  T* pnew;
-  T* q;
-  const uint8_t* fixed;
-  double* scal;
-  double* part;
-  unsigned* ticket;
-};
-
-template <class T, bool MASK>
-__device__ void grid_cg_interior(const GridCoef<T>& P, int item, const CgStep<T>& A, T beta,
-                                 DotAcc<T>& dot, typename Vec4<T>::type* sm) {
-  using V4 = typename Vec4<T>::type;
-  const int tid = threadIdx.x;
-  const int nx = P.nx, ny = P.ny, nz = P.nz;
-  const int tx = item % P.tiles_x;
-  const int rest = item / P.tiles_x;
-  const int ty = rest % P.tiles_y;
-  const int tzi = rest / P.tiles_y;
-  const int x0 = 1 + tx * GR_TX, y0 = 1 + ty * GR_TY;
-  const int zs = 1 + tzi * P.tz;
-  const int ze = min(zs + P.tz, nz - 1);
-  const int lx = tid % GR_TX, ly = tid / GR_TX;
-  const int x = x0 + lx, yy = y0 + ly;
-  const bool own = (x <= nx - 2) && (yy <= ny - 2);
-  const int64_t plane_nodes = (int64_t)nx * ny;
-
-  int64_t soff[GR_SLOTS];  // node offset within a plane, -1: outside the grid / no slot
-  bool sown[GR_SLOTS];     // the slot's node is an output node of this tile (x, y)
-#pragma unroll
-  for (int k = 0; k < GR_SLOTS; ++k) {
-    const int s = tid + k * GR_THREADS;
-    soff[k] = -1;
-    sown[k] = false;
-    if (s < GR_PLANE) {
-      const int hx = s % GR_PX, hy = s / GR_PX;
-      const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
-      if (gx < nx && gy < ny) soff[k] = gx + (int64_t)nx * gy;
-      sown[k] = hx >= 1 && hx <= GR_TX && hy >= 1 && hy <= GR_TY && gx <= nx - 2 && gy <= ny - 2;
+  if constexpr (DOT) {
+    double v[1] = {dot.value()};
+    block_reduce_store<1, GR_THREADS>(v, D.part + blockIdx.x);
+    if (!last_cta(D.ticket)) return;
+    double w[1] = {0.0};
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += GR_THREADS) w[0] += __ldcg(D.part + i);
+    __shared__ double out[1];
+    block_reduce_store<1, GR_THREADS>(w, out);
+    if (threadIdx.x == 0) {
+      const double pq = out[0];
+      D.scal[SCAL_PQ] = pq;
+      const bool bad = !(pq > 0.0) || !isfinite(pq) || D.scal[SCAL_FLAG] != 0.0;
+      if (bad) D.scal[SCAL_FLAG] = 1.0;
+      D.scal[SCAL_ALPHA] = bad ? 0.0 : D.scal[SCAL_RZ] / pq;
     }
-  }
-  // one plane ahead in registers: r, dinv, p_old and the mask bits of the staged slots
-  T rr[GR_SLOTS][3], dd[GR_SLOTS][3], po[GR_SLOTS][3];
-  int fb[GR_SLOTS];
-  auto load_plane = [&](int p) {
-#pragma unroll
-    for (int k = 0; k < GR_SLOTS; ++k) {
-      fb[k] = 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) rr[k][d] = dd[k][d] = po[k][d] = T(0);
-      if (soff[k] >= 0 && p <= ze) {
-        const int64_t base = 3 * (soff[k] + plane_nodes * p);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          rr[k][d] = __ldg(A.r + base + d);
-          dd[k][d] = __ldg(A.dinv + base + d);
-          po[k][d] = __ldg(A.pold + base + d);
-          if (MASK && __ldg(A.fixed + base + d)) fb[k] |= 1 << d;
-        }
-      }
-    }
-  };
-  auto store_plane = [&](V4* buf, int p) {
-    const bool out_plane = p >= zs && p < ze;
-#pragma unroll
-    for (int k = 0; k < GR_SLOTS; ++k) {
-      const int s = tid + k * GR_THREADS;
-      if (s < GR_PLANE) {
-        T pn[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) pn[d] = fma(beta, po[k][d], rr[k][d] * dd[k][d]);
-        if (sown[k] && out_plane) {
-          const int64_t base = 3 * (soff[k] + plane_nodes * p);
-#pragma unroll
-          for (int d = 0; d < 3; ++d) A.pnew[base + d] = pn[d];
-        }
-        buf[s] = make4<T>((fb[k] & 1) ? T(0) : pn[0], (fb[k] & 2) ? T(0) : pn[1],
-                          (fb[k] & 4) ? T(0) : pn[2]);
-      }
-    }
-  };
-
-  T accM[3], accP[3], accN[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) accM[a] = accP[a] = accN[a] = T(0);
-  const int c0 = (lx + 1) + GR_PX * (ly + 1);
-  T prev[3], ctr[3] = {T(0), T(0), T(0)};
-
-  auto emit = [&](int z, const T (&acc)[3], const T (&pc)[3]) {
-    if (!own || z < zs || z >= ze) return;
-    const int64_t base = 3 * (x + (int64_t)nx * yy + plane_nodes * z);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      T pv = pc[d], qv = acc[d];
-      if (MASK && __ldg(A.fixed + base + d)) {
-        pv = __ldcg(A.pnew + base + d);  // written by this CTA's staging, before a barrier
-        qv = pv;
-      }
-      A.q[base + d] = qv;
-      dot.add(pv, qv);
-    }
-  };
-
-  V4* buf0 = sm;
-  V4* buf1 = sm + GR_PLANE;
-  load_plane(zs - 1);
-  store_plane(buf0, zs - 1);
-  load_plane(zs);
-  __syncthreads();
-  {
-    const V4 c = buf0[c0];
-    prev[0] = c.x;
-    prev[1] = c.y;
-    prev[2] = c.z;
-  }
-  for (int p = zs - 1; p <= ze; ++p) {
-    const bool even = ((p - zs + 1) & 1) == 0;
-    V4* cur = even ? buf0 : buf1;
-    V4* nxt = even ? buf1 : buf0;
-    const T pc[3] = {ctr[0], ctr[1], ctr[2]};
-    stencil_plane<T>(P, cur, c0, accM, accP, accN, prev, ctr);
-    emit(p - 1, accM, pc);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      accM[a] = accP[a];
-      accP[a] = accN[a];
-      accN[a] = T(0);
-    }
-    if (p + 1 <= ze) store_plane(nxt, p + 1);
-    load_plane(p + 2);
-    __syncthreads();
-  }
-}
-
-template <class T, bool MASK>
-__device__ void grid_cg_boundary(const GridCoef<T>& P, int64_t t0, const CgStep<T>& A, T beta,
-                                 DotAcc<T>& dot, T* ke) {
-  for (int i = threadIdx.x; i < 8 * 8 * 9; i += blockDim.x) ke[i] = (&P.ke[0][0][0][0])[i];
-  __syncthreads();
-  const int64_t t = t0 + threadIdx.x;
-  if (t >= P.n_boundary) return;
-  const int nx = P.nx, ny = P.ny, nz = P.nz;
-  int x, yy, z;
-  boundary_node(t, nx, ny, nz, x, yy, z);
-  auto pval = [&](int64_t dof) {
-    return fma(beta, __ldg(A.pold + dof), __ldg(A.r + dof) * __ldg(A.dinv + dof));
-  };
-  T acc[3] = {T(0), T(0), T(0)};
-  for (int o = 0; o < 8; ++o) {
-    const int ox = o & 1, oy = (o >> 1) & 1, oz = o >> 2;
-    const int cx = x - ox, cy = yy - oy, cz = z - oz;
-    if (cx < 0 || cy < 0 || cz < 0 || cx >= nx - 1 || cy >= ny - 1 || cz >= nz - 1) continue;
-    const T* kr = ke + o * 72;
-#pragma unroll
-    for (int cm = 0; cm < 8; ++cm) {
-      const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
-                                                         (int64_t)ny * (cz + (cm >> 2)));
-      T v[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        v[d] = pval(3 * g + d);
-        if (MASK && __ldg(A.fixed + 3 * g + d)) v[d] = T(0);
-      }
-      const T* k9 = kr + cm * 9;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) acc[a] = fma(k9[3 * a + 2], v[2], fma(k9[3 * a + 1], v[1], fma(k9[3 * a], v[0], acc[a])));
-    }
-  }
-  const int64_t base = 3 * (x + (int64_t)nx * (yy + (int64_t)ny * z));
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const T pv = pval(base + d);
-    T qv = acc[d];
-    if (MASK && __ldg(A.fixed + base + d)) qv = pv;
-    A.pnew[base + d] = pv;
-    A.q[base + d] = qv;
-    dot.add(pv, qv);
-  }
-}
-
-template <class T, bool MASK>
-__global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
-    grid_cg_kernel(const __grid_constant__ GridCoef<T> P, const __grid_constant__ CgStep<T> A) {
-  using V4 = typename Vec4<T>::type;
-  __shared__ V4 sm[2 * GR_PLANE];
-  const T beta = (T)A.scal[SCAL_BETA];
-  DotAcc<T> dot;
-  const int b = blockIdx.x;
-  if (b < P.n_boundary_ctas) {
-    grid_cg_boundary<T, MASK>(P, (int64_t)b * GR_THREADS, A, beta, dot, reinterpret_cast<T*>(sm));
-  } else {
-    grid_cg_interior<T, MASK>(P, b - P.n_boundary_ctas, A, beta, dot, sm);
-  }
-  double v[1] = {dot.value()};
-  block_reduce_store<1, GR_THREADS>(v, A.part + blockIdx.x);
-  if (!last_cta(A.ticket)) return;
-  double w[1] = {0.0};
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += GR_THREADS) w[0] += __ldcg(A.part + i);
-  __shared__ double out[1];
-  block_reduce_store<1, GR_THREADS>(w, out);
-  if (threadIdx.x == 0) {
-    const double pq = out[0];
-    A.scal[SCAL_PQ] = pq;
-    const bool bad = !(pq > 0.0) || !isfinite(pq) || A.scal[SCAL_FLAG] != 0.0;
-    if (bad) A.scal[SCAL_FLAG] = 1.0;
-    A.scal[SCAL_ALPHA] = bad ? 0.0 : A.scal[SCAL_RZ] / pq;
   }
 }
 
@@ -700,13 +523,15 @@ static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, con
   if (n == 0) return TG_OK;
   const T* in = (mode == TG_MODE_HVP) ? v : u;
   const unsigned grid = (unsigned)n;
+  const GridDot D{nullptr, nullptr, nullptr};
   if (mode == TG_MODE_HVP) {
     if (fixed)
-      grid_le_kernel<T, TG_MODE_HVP, true><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
+      grid_le_kernel<T, TG_MODE_HVP, true, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y, D);
     else
-      grid_le_kernel<T, TG_MODE_HVP, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
+      grid_le_kernel<T, TG_MODE_HVP, false, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y, D);
   } else {
-    grid_le_kernel<T, TG_MODE_RESIDUAL, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y);
+    grid_le_kernel<T, TG_MODE_RESIDUAL, false, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed,
+                                                                                   y, D);
   }
   return launch_check("grid linear-elastic kernel");
 }
@@ -716,22 +541,23 @@ int64_t grid_cg_ctas(const tg_block_plan* plan) {
   return grid_setup<float>(plan, 1.0, 1.0, P);
 }
 
-int launch_grid_cg(const tg_block_plan* plan, int prec, double mu, double lam, const void* r,
-                   const void* dinv, const void* pold, void* pnew, void* q,
-                   const uint8_t* fixed, double* scal, double* part, unsigned* ticket,
-                   cudaStream_t st) {
+int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double lam,
+                        const void* p, const uint8_t* fixed, void* q, double* scal, double* part,
+                        unsigned* ticket, cudaStream_t st) {
   auto go = [&](auto t) -> int {
     using T = decltype(t);
     GridCoef<T> P;
     const int64_t n = grid_setup<T>(plan, mu, lam, P);
     if (n <= 0) return set_error(TG_ERR_VALUE, "grid CG: empty or too large grid");
-    CgStep<T> A{(const T*)r, (const T*)dinv, (const T*)pold, (T*)pnew, (T*)q, fixed, scal, part,
-                ticket};
+    const GridDot D{scal, part, ticket};
+    const T* in = (const T*)p;
     if (fixed)
-      grid_cg_kernel<T, true><<<(unsigned)n, GR_THREADS, 0, st>>>(P, A);
+      grid_le_kernel<T, TG_MODE_HVP, true, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
+          P, in, in, fixed, (T*)q, D);
     else
-      grid_cg_kernel<T, false><<<(unsigned)n, GR_THREADS, 0, st>>>(P, A);
-    return launch_check("grid CG step");
+      grid_le_kernel<T, TG_MODE_HVP, false, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
+          P, in, in, fixed, (T*)q, D);
+    return launch_check("grid HVP with p.q");
   };
   return prec == TG_F32 ? go(0.f) : go(0.0);
 }

@@ -280,7 +280,6 @@ __global__ void cg_init_final_kernel(const double* __restrict__ part, double* __
     scal[SCAL_RZ] = out[0];
     scal[SCAL_RR] = out[1];
     scal[SCAL_FLAG] = 0.0;
-    scal[SCAL_BETA] = 0.0;  // the fused grid step rebuilds p = dinv r + 0 p_old
   }
 }
 
@@ -597,18 +596,14 @@ namespace tg {
 
 struct CgBuffers {
   void *r, *p, *q, *dinv, *apply_ws;
-  void* p2;    // second search-direction buffer of the fused grid step (ping-pong)
-  int parity;  // the current direction is (parity ? p2 : p)
-  bool grid;   // fused grid step (structured-brick linear elasticity)
+  bool grid;  // structured-brick linear elasticity: the HVP launch also forms p.q
   double *part, *scal;
   unsigned* ticket;  // [2] last-CTA arrival counters of the p.q and update kernels
   size_t apply_bytes;
-  void* pcur() const { return parity ? p2 : p; }
-  void* pnext() const { return parity ? p : p2; }
 };
 
 // The operator is linear elasticity on a structured brick whose plan carries the grid:
-// CG iterations use the fused grid step.
+// the CG's HVP runs as the grid stencil and forms p.q and alpha in the same launch.
 static bool grid_op(const tg_operator_desc* op) {
   return !op->csr_data && op->plan && op->elem == TG_HEX8 && op->mat.kind == TG_LINEAR_ELASTIC &&
          op->mat.elem_param == nullptr && op->plan->grid_nodes[0] > 0 &&
@@ -625,7 +620,7 @@ static int64_t cg_part_doubles(const tg_operator_desc* op) {
 static size_t cg_bytes(const tg_operator_desc* op) {
   const int64_t n = op_ndofs(op);
   const size_t vs = align256((size_t)n * prec_size(op->prec));
-  return (grid_op(op) ? 5 : 4) * vs + align256(tg_operator_workspace_bytes(op)) +
+  return 4 * vs + align256(tg_operator_workspace_bytes(op)) +
          align256((size_t)cg_part_doubles(op) * sizeof(double)) +
          align256(SCAL_N * sizeof(double)) + align256(2 * sizeof(unsigned));
 }
@@ -636,12 +631,10 @@ static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
   CgBuffers b;
   const size_t vb = (size_t)n * prec_size(op->prec);
   b.grid = grid_op(op);
-  b.parity = 0;
   b.r = c.take(vb);
   b.p = c.take(vb);
   b.dinv = c.take(vb);
   b.q = c.take(vb);
-  b.p2 = b.grid ? c.take(vb) : nullptr;
   b.apply_bytes = tg_operator_workspace_bytes(op);
   b.apply_ws = c.take(b.apply_bytes);
   b.part = (double*)c.take((size_t)cg_part_doubles(op) * sizeof(double));
@@ -659,7 +652,7 @@ static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* 
   axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
   inv_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, diag, (T*)B.dinv);
   cg_init_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, (const T*)B.r, (const T*)B.dinv,
-                                                        (T*)B.pcur(), B.part);
+                                                        (T*)B.p, B.part);
   cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
   TG_TRY(cuda_check(cudaMemsetAsync(B.ticket, 0, 2 * sizeof(unsigned), st), "cg: counters"));
   return launch_check("cg restart");
@@ -669,19 +662,14 @@ template <class T>
 static int cg_iteration(const tg_operator_desc* op, T* x, const T* diag, CgBuffers& B,
                         cudaStream_t st) {
   const int64_t n = op_ndofs(op);
-  if (B.grid) {
-    // fused: p = dinv r + beta p_old, q = A p, alpha (one kernel); then the update
-    TG_TRY(launch_grid_cg(op->plan, op->prec, op->mat.p0, op->mat.p1, B.r, B.dinv, B.pcur(),
-                          B.pnext(), B.q, op->fixed, B.scal, B.part, B.ticket, st));
-    B.parity ^= 1;
-    cg_update_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(
-        n, B.scal, x, (T*)B.r, (const T*)B.pcur(), (const T*)B.q, (const T*)B.dinv, B.part,
-        B.ticket + 1);
-    return launch_check("cg iteration (grid)");
+  if (B.grid) {  // q = A p with p.q and alpha in the same launch
+    TG_TRY(launch_grid_hvp_dot(op->plan, op->prec, op->mat.p0, op->mat.p1, B.p, op->fixed, B.q,
+                               B.scal, B.part, B.ticket, st));
+  } else {
+    TG_TRY(tg_operator_apply(op, B.p, B.q, B.apply_ws, B.apply_bytes, st));
+    cg_pq_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n,
+                                                        B.part, B.scal, B.ticket);
   }
-  TG_TRY(tg_operator_apply(op, B.p, B.q, B.apply_ws, B.apply_bytes, st));
-  cg_pq_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>((const T*)B.p, (const T*)B.q, n, B.part,
-                                                      B.scal, B.ticket);
   cg_update_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, B.scal, x, (T*)B.r,
                                                           (const T*)B.p, (const T*)B.q,
                                                           (const T*)B.dinv, B.part, B.ticket + 1);
@@ -714,9 +702,7 @@ static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag
   int rc = TG_OK;
   while (*iters < max_iter) {
     const int k = (max_iter - *iters) < check_every ? (max_iter - *iters) : check_every;
-    // a captured run must leave the direction buffers' parity as it found it (the fused
-    // grid step alternates them): graphs of an even number of iterations only
-    if (can_capture && k == check_every && (!B.grid || k % 2 == 0)) {
+    if (can_capture && k == check_every) {
       if (!exec || graph_len != k) {
         cudaGraph_t graph;
         rc = cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cg: capture");

@@ -21,13 +21,12 @@ int launch_hex_le_f32x2(const tg_block_plan* plan, int mode, const float* coords
 int launch_grid_le(const tg_block_plan* plan, int prec, int mode, const void* u, const void* v,
                    const uint8_t* fixed, void* y, double mu, double lam, cudaStream_t st);
 
-// Fused Jacobi-CG step on a structured brick (see grid.cu): p = dinv r + beta p_old,
-// q = A p (masked), alpha = rz / (p . q) into scal; part needs grid_cg_ctas(plan)
-// doubles, ticket one zeroed counter.
+// HVP q = A p on a structured brick with the CG dot: alpha = rz / (p . q) into scal
+// (SCAL_* slots of the CG), through per-CTA partials in part (grid_cg_ctas(plan)
+// doubles) and a zeroed arrival counter ticket.
 int64_t grid_cg_ctas(const tg_block_plan* plan);
-int launch_grid_cg(const tg_block_plan* plan, int prec, double mu, double lam, const void* r,
-                   const void* dinv, const void* pold, void* pnew, void* q,
-                   const uint8_t* fixed, double* scal, double* part, unsigned* ticket,
-                   cudaStream_t st);
+int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double lam,
+                        const void* p, const uint8_t* fixed, void* q, double* scal, double* part,
+                        unsigned* ticket, cudaStream_t st);
 
 }  // namespace tg

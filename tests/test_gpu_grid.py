@@ -114,9 +114,9 @@ def test_grid_brick_128_properties(cuda):
 
 @pytest.mark.parametrize("check_every", [10, 7])
 def test_grid_cg_matches_element_cg_and_is_deterministic(cuda, check_every):
-    """The fused grid CG step (p update, HVP and p.q in one kernel) against the CG on
-    the element-block HVP: same tolerance reached, same solution to 1e-8; FP64 and
-    mixed precision; repeated solves bitwise equal (odd check_every: no graph)."""
+    """CG on the grid stencil (the HVP launch also forms p.q and alpha) against the CG
+    on the element-block HVP: same tolerance reached, same solution to 1e-8; FP64 and
+    mixed precision; repeated solves bitwise equal (check_every 10 and 7)."""
     from tatva_gb300 import solvers
 
     c, e = om.brick(20, 12, 10, lengths=(2.0, 1.2, 1.0))

@@ -95,13 +95,29 @@ __device__ __forceinline__ typename Vec4<T>::type make4(T a, T b, T c) {
   return r;
 }
 
-// input value of dof (node g, comp d): v read as 0 on fixed dofs when MASK
-template <class T, bool MASK>
-__device__ __forceinline__ T load_in(const T* __restrict__ in, const uint8_t* __restrict__ fixed,
-                                     int64_t dof) {
-  T x = __ldg(in + dof);
-  if (MASK && __ldg(fixed + dof)) x = T(0);
-  return x;
+// Dirichlet masks: none, one byte per dof (the C ABI's `fixed`), or one byte per node
+// with bit d set when dof 3 n + d is fixed (packed once per solve by the CG, so that a
+// node's mask is one load instead of three)
+constexpr int MASK_NONE = 0, MASK_DOF = 1, MASK_NODE = 2;
+
+// bit d of the mask of node g (0: free)
+template <int MK>
+__device__ __forceinline__ int mask_bits(const uint8_t* __restrict__ fixed, int64_t g) {
+  if constexpr (MK == MASK_DOF) {
+    return (__ldg(fixed + 3 * g) != 0) | (__ldg(fixed + 3 * g + 1) != 0) << 1 |
+           (__ldg(fixed + 3 * g + 2) != 0) << 2;
+  } else if constexpr (MK == MASK_NODE) {
+    return __ldg(fixed + g);
+  } else {
+    return 0;
+  }
+}
+
+// pack the per-dof mask into one byte per node
+__global__ void pack_node_mask_kernel(const uint8_t* __restrict__ fixed, int64_t n_nodes,
+                                      uint8_t* __restrict__ out) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n_nodes) out[g] = (uint8_t)mask_bits<MASK_DOF>(fixed, g);
 }
 
 // One input plane's contributions to the outputs below (accM, z - 1), at (accP, z) and
@@ -186,7 +202,7 @@ __device__ __forceinline__ void stencil_plane(const GridCoef<T>& P,
 
 // Interior tile: thread (lx, ly) owns node column (x0 + lx, y0 + ly), planes
 // [zs, ze) of output.
-template <class T, int MODE, bool MASK, bool DOT>
+template <class T, int MODE, int MK, bool DOT>
 __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restrict__ in,
                               const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
                               T* __restrict__ y, typename Vec4<T>::type* sm, DotAcc<T>& dot) {
@@ -222,9 +238,13 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
 #pragma unroll
       for (int d = 0; d < 3; ++d) r[k][d] = T(0);
       if (soff[k] >= 0 && p <= ze) {
-        const int64_t base = 3 * (soff[k] + plane_nodes * p);
+        const int64_t g = soff[k] + plane_nodes * p;
+        const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) r[k][d] = load_in<T, MASK>(in, fixed, base + d);
+        for (int d = 0; d < 3; ++d) {
+          const T v = __ldg(in + 3 * g + d);
+          r[k][d] = (m >> d & 1) ? T(0) : v;
+        }
       }
     }
   };
@@ -249,11 +269,12 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   // which is also their output) enters the CTA's dot partial
   auto emit = [&](int z, const T (&acc)[3], const T (&pc)[3]) {
     if (!own || z < zs || z >= ze) return;
-    const int64_t base = 3 * (x + (int64_t)nx * yy + plane_nodes * z);
+    const int64_t g = x + (int64_t)nx * yy + plane_nodes * z, base = 3 * g;
+    const int m = mask_bits<MK>(fixed, g);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T val = acc[d], pv = pc[d];
-      if (fixed && __ldg(fixed + base + d)) {
+      if (m >> d & 1) {
         val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
         pv = val;
       }
@@ -337,7 +358,7 @@ __device__ __forceinline__ void boundary_node(int64_t t, int nx, int ny, int nz,
   z = 1 + (int)(r / (ny - 2));
 }
 
-template <class T, int MODE, bool MASK, bool DOT>
+template <class T, int MODE, int MK, bool DOT>
 __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restrict__ in,
                               const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
                               T* __restrict__ y, T* ke, DotAcc<T>& dot) {
@@ -358,21 +379,23 @@ __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restr
     for (int cm = 0; cm < 8; ++cm) {
       const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
                                                          (int64_t)ny * (cz + (cm >> 2)));
-      const T v0 = load_in<T, MASK>(in, fixed, 3 * g);
-      const T v1 = load_in<T, MASK>(in, fixed, 3 * g + 1);
-      const T v2 = load_in<T, MASK>(in, fixed, 3 * g + 2);
+      const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
+      const T v0 = (m & 1) ? T(0) : __ldg(in + 3 * g);
+      const T v1 = (m & 2) ? T(0) : __ldg(in + 3 * g + 1);
+      const T v2 = (m & 4) ? T(0) : __ldg(in + 3 * g + 2);
       const T* k9 = kr + cm * 9;
 #pragma unroll
       for (int a = 0; a < 3; ++a) acc[a] = fma(k9[3 * a + 2], v2, fma(k9[3 * a + 1], v1, fma(k9[3 * a], v0, acc[a])));
     }
   }
-  const int64_t base = 3 * (x + (int64_t)nx * (yy + (int64_t)ny * z));
+  const int64_t gn = x + (int64_t)nx * (yy + (int64_t)ny * z), base = 3 * gn;
+  const int mn = mask_bits<MK>(fixed, gn);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     T val = acc[d];
     T pv = T(0);
     if constexpr (DOT) pv = __ldg(in + base + d);
-    if (fixed && __ldg(fixed + base + d)) {
+    if (mn >> d & 1) {
       val = (MODE == TG_MODE_HVP) ? __ldg(vin + base + d) : T(0);
       pv = val;
     }
@@ -392,7 +415,7 @@ struct GridDot {
 // fixed rows are the identity, so they add p^2) -- per CTA in a fixed order, the CTAs'
 // partials added by the CTA that arrives last in index order -- and stores
 // alpha = rz / (p.q) for the CG update (breakdown flag when p.q <= 0 or not finite).
-template <class T, int MODE, bool MASK, bool DOT>
+template <class T, int MODE, int MK, bool DOT>
 __global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
     grid_le_kernel(const __grid_constant__ GridCoef<T> P, const T* __restrict__ in,
                    const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
@@ -403,10 +426,10 @@ __global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
   // boundary CTAs first: they start with the first wave and overlap the interior tiles
   const int b = blockIdx.x;
   if (b < P.n_boundary_ctas) {
-    grid_boundary<T, MODE, MASK, DOT>(P, (int64_t)b * GR_THREADS, in, vin, fixed, y,
+    grid_boundary<T, MODE, MK, DOT>(P, (int64_t)b * GR_THREADS, in, vin, fixed, y,
                                       reinterpret_cast<T*>(sm), dot);
   } else {
-    grid_interior<T, MODE, MASK, DOT>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm, dot);
+    grid_interior<T, MODE, MK, DOT>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm, dot);
   }
   if constexpr (DOT) {
     double v[1] = {dot.value()};
@@ -526,12 +549,17 @@ static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, con
   const GridDot D{nullptr, nullptr, nullptr};
   if (mode == TG_MODE_HVP) {
     if (fixed)
-      grid_le_kernel<T, TG_MODE_HVP, true, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y, D);
+      grid_le_kernel<T, TG_MODE_HVP, MASK_DOF, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed,
+                                                                                  y, D);
     else
-      grid_le_kernel<T, TG_MODE_HVP, false, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed, y, D);
+      grid_le_kernel<T, TG_MODE_HVP, MASK_NONE, false><<<grid, GR_THREADS, 0, st>>>(P, in, v,
+                                                                                   fixed, y, D);
+  } else if (fixed) {
+    grid_le_kernel<T, TG_MODE_RESIDUAL, MASK_DOF, false><<<grid, GR_THREADS, 0, st>>>(
+        P, in, v, fixed, y, D);
   } else {
-    grid_le_kernel<T, TG_MODE_RESIDUAL, false, false><<<grid, GR_THREADS, 0, st>>>(P, in, v, fixed,
-                                                                                   y, D);
+    grid_le_kernel<T, TG_MODE_RESIDUAL, MASK_NONE, false><<<grid, GR_THREADS, 0, st>>>(
+        P, in, v, fixed, y, D);
   }
   return launch_check("grid linear-elastic kernel");
 }
@@ -541,9 +569,14 @@ int64_t grid_cg_ctas(const tg_block_plan* plan) {
   return grid_setup<float>(plan, 1.0, 1.0, P);
 }
 
+int pack_node_mask(const uint8_t* fixed, int64_t n_nodes, uint8_t* out, cudaStream_t st) {
+  pack_node_mask_kernel<<<grid_for(n_nodes, 256), 256, 0, st>>>(fixed, n_nodes, out);
+  return launch_check("pack node mask");
+}
+
 int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double lam,
-                        const void* p, const uint8_t* fixed, void* q, double* scal, double* part,
-                        unsigned* ticket, cudaStream_t st) {
+                        const void* p, const uint8_t* node_mask, void* q, double* scal,
+                        double* part, unsigned* ticket, cudaStream_t st) {
   auto go = [&](auto t) -> int {
     using T = decltype(t);
     GridCoef<T> P;
@@ -551,12 +584,12 @@ int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double l
     if (n <= 0) return set_error(TG_ERR_VALUE, "grid CG: empty or too large grid");
     const GridDot D{scal, part, ticket};
     const T* in = (const T*)p;
-    if (fixed)
-      grid_le_kernel<T, TG_MODE_HVP, true, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
-          P, in, in, fixed, (T*)q, D);
+    if (node_mask)
+      grid_le_kernel<T, TG_MODE_HVP, MASK_NODE, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
+          P, in, in, node_mask, (T*)q, D);
     else
-      grid_le_kernel<T, TG_MODE_HVP, false, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
-          P, in, in, fixed, (T*)q, D);
+      grid_le_kernel<T, TG_MODE_HVP, MASK_NONE, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
+          P, in, in, node_mask, (T*)q, D);
     return launch_check("grid HVP with p.q");
   };
   return prec == TG_F32 ? go(0.f) : go(0.0);

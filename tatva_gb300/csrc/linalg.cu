@@ -597,6 +597,7 @@ namespace tg {
 struct CgBuffers {
   void *r, *p, *q, *dinv, *apply_ws;
   bool grid;  // structured-brick linear elasticity: the HVP launch also forms p.q
+  uint8_t* nmask;  // grid: the Dirichlet mask packed to one byte per node (or NULL)
   double *part, *scal;
   unsigned* ticket;  // [2] last-CTA arrival counters of the p.q and update kernels
   size_t apply_bytes;
@@ -620,7 +621,8 @@ static int64_t cg_part_doubles(const tg_operator_desc* op) {
 static size_t cg_bytes(const tg_operator_desc* op) {
   const int64_t n = op_ndofs(op);
   const size_t vs = align256((size_t)n * prec_size(op->prec));
-  return 4 * vs + align256(tg_operator_workspace_bytes(op)) +
+  const size_t mask_bytes = (grid_op(op) && op->fixed) ? align256((size_t)op->n_nodes) : 0;
+  return 4 * vs + mask_bytes + align256(tg_operator_workspace_bytes(op)) +
          align256((size_t)cg_part_doubles(op) * sizeof(double)) +
          align256(SCAL_N * sizeof(double)) + align256(2 * sizeof(unsigned));
 }
@@ -635,6 +637,7 @@ static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
   b.p = c.take(vb);
   b.dinv = c.take(vb);
   b.q = c.take(vb);
+  b.nmask = (b.grid && op->fixed) ? (uint8_t*)c.take((size_t)op->n_nodes) : nullptr;
   b.apply_bytes = tg_operator_workspace_bytes(op);
   b.apply_ws = c.take(b.apply_bytes);
   b.part = (double*)c.take((size_t)cg_part_doubles(op) * sizeof(double));
@@ -655,6 +658,7 @@ static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* 
                                                         (T*)B.p, B.part);
   cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
   TG_TRY(cuda_check(cudaMemsetAsync(B.ticket, 0, 2 * sizeof(unsigned), st), "cg: counters"));
+  if (B.nmask) TG_TRY(pack_node_mask(op->fixed, op->n_nodes, B.nmask, st));
   return launch_check("cg restart");
 }
 
@@ -663,7 +667,7 @@ static int cg_iteration(const tg_operator_desc* op, T* x, const T* diag, CgBuffe
                         cudaStream_t st) {
   const int64_t n = op_ndofs(op);
   if (B.grid) {  // q = A p with p.q and alpha in the same launch
-    TG_TRY(launch_grid_hvp_dot(op->plan, op->prec, op->mat.p0, op->mat.p1, B.p, op->fixed, B.q,
+    TG_TRY(launch_grid_hvp_dot(op->plan, op->prec, op->mat.p0, op->mat.p1, B.p, B.nmask, B.q,
                                B.scal, B.part, B.ticket, st));
   } else {
     TG_TRY(tg_operator_apply(op, B.p, B.q, B.apply_ws, B.apply_bytes, st));

@@ -25,8 +25,11 @@ int launch_grid_le(const tg_block_plan* plan, int prec, int mode, const void* u,
 // (SCAL_* slots of the CG), through per-CTA partials in part (grid_cg_ctas(plan)
 // doubles) and a zeroed arrival counter ticket.
 int64_t grid_cg_ctas(const tg_block_plan* plan);
+// node_mask: NULL, or one byte per node, bit d set when dof 3 n + d is fixed
+// (pack_node_mask from the C ABI's per-dof mask).
 int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double lam,
-                        const void* p, const uint8_t* fixed, void* q, double* scal, double* part,
-                        unsigned* ticket, cudaStream_t st);
+                        const void* p, const uint8_t* node_mask, void* q, double* scal,
+                        double* part, unsigned* ticket, cudaStream_t st);
+int pack_node_mask(const uint8_t* fixed, int64_t n_nodes, uint8_t* out, cudaStream_t st);
 
 }  // namespace tg

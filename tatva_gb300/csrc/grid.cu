@@ -232,27 +232,29 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
       if (gx < nx && gy < ny) soff[k] = gx + (int64_t)nx * gy;
     }
   }
-  auto load_plane = [&](int p, T (&r)[GR_SLOTS][3]) {
+  // raw values and mask bits stay in registers until the plane is stored, so that no
+  // load is waited for before then (the prefetch distance is two planes)
+  auto load_plane = [&](int p, T (&r)[GR_SLOTS][3], int (&m)[GR_SLOTS]) {
 #pragma unroll
     for (int k = 0; k < GR_SLOTS; ++k) {
+      m[k] = 0;
 #pragma unroll
       for (int d = 0; d < 3; ++d) r[k][d] = T(0);
       if (soff[k] >= 0 && p <= ze) {
         const int64_t g = soff[k] + plane_nodes * p;
-        const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
+        if (MODE == TG_MODE_HVP) m[k] = mask_bits<MK>(fixed, g);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const T v = __ldg(in + 3 * g + d);
-          r[k][d] = (m >> d & 1) ? T(0) : v;
-        }
+        for (int d = 0; d < 3; ++d) r[k][d] = __ldg(in + 3 * g + d);
       }
     }
   };
-  auto store_plane = [&](V4* buf, const T (&r)[GR_SLOTS][3]) {
+  auto store_plane = [&](V4* buf, const T (&r)[GR_SLOTS][3], const int (&m)[GR_SLOTS]) {
 #pragma unroll
     for (int k = 0; k < GR_SLOTS; ++k) {
       const int s = tid + k * GR_THREADS;
-      if (s < GR_PLANE) buf[s] = make4<T>(r[k][0], r[k][1], r[k][2]);
+      if (s < GR_PLANE)
+        buf[s] = make4<T>((m[k] & 1) ? T(0) : r[k][0], (m[k] & 2) ? T(0) : r[k][1],
+                          (m[k] & 4) ? T(0) : r[k][2]);
     }
   };
 
@@ -267,10 +269,14 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   // pc: the node's own input (the column's value in the output plane, masked): with
   // DOT the product input . output of the owned dofs (fixed dofs: their unmasked input,
   // which is also their output) enters the CTA's dot partial
-  auto emit = [&](int z, const T (&acc)[3], const T (&pc)[3]) {
+  // the output node's mask bits, loaded one plane before its emission
+  auto out_mask = [&](int z) {
+    return (own && z >= zs && z < ze) ? mask_bits<MK>(fixed, x + (int64_t)nx * yy + plane_nodes * z)
+                                      : 0;
+  };
+  auto emit = [&](int z, const T (&acc)[3], const T (&pc)[3], int m) {
     if (!own || z < zs || z >= ze) return;
     const int64_t g = x + (int64_t)nx * yy + plane_nodes * z, base = 3 * g;
-    const int m = mask_bits<MK>(fixed, g);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T val = acc[d], pv = pc[d];
@@ -286,11 +292,13 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   V4* buf0 = sm;
   V4* buf1 = sm + GR_PLANE;
   T rA[GR_SLOTS][3], rB[GR_SLOTS][3];
+  int mA[GR_SLOTS], mB[GR_SLOTS];
   // prologue: plane zs - 1 into buf0; zs in flight in rB, zs + 1 in rA
-  load_plane(zs - 1, rA);
-  store_plane(buf0, rA);
-  load_plane(zs, rB);
-  load_plane(zs + 1, rA);
+  load_plane(zs - 1, rA, mA);
+  store_plane(buf0, rA, mA);
+  load_plane(zs, rB, mB);
+  load_plane(zs + 1, rA, mA);
+  int m_out = out_mask(zs - 1);  // mask of the node emitted after the next plane
   __syncthreads();
   {  // the first plane's step then sees no z difference (its outputs are discarded)
     const V4 c = buf0[c0];
@@ -302,30 +310,34 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   ctr[0] = ctr[1] = ctr[2] = T(0);
   for (int p = zs - 1; p <= ze; p += 2) {
     T pc[3] = {ctr[0], ctr[1], ctr[2]};
+    int m_now = m_out;
+    m_out = out_mask(p);
     plane_step(buf0);
-    emit(p - 1, accM, pc);
+    emit(p - 1, accM, pc, m_now);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       accM[a] = accP[a];
       accP[a] = accN[a];
       accN[a] = T(0);
     }
-    store_plane(buf1, rB);
-    load_plane(p + 3, rB);
+    store_plane(buf1, rB, mB);
+    load_plane(p + 3, rB, mB);
     __syncthreads();
     if (p + 1 > ze) break;
 #pragma unroll
     for (int a = 0; a < 3; ++a) pc[a] = ctr[a];
+    m_now = m_out;
+    m_out = out_mask(p + 1);
     plane_step(buf1);
-    emit(p, accM, pc);
+    emit(p, accM, pc, m_now);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       accM[a] = accP[a];
       accP[a] = accN[a];
       accN[a] = T(0);
     }
-    store_plane(buf0, rA);
-    load_plane(p + 4, rA);
+    store_plane(buf0, rA, mA);
+    load_plane(p + 4, rA, mA);
     __syncthreads();
   }
 }

@@ -54,7 +54,7 @@ namespace tg {
 #define TG_GRID_MINB 3
 #endif
 #ifndef TG_GRID_TZ
-#define TG_GRID_TZ 16
+#define TG_GRID_TZ 11
 #endif
 constexpr int GR_TX = 32, GR_TY = TG_GRID_TY, GR_THREADS = GR_TX * GR_TY;
 constexpr int GR_PX = GR_TX + 2, GR_PY = GR_TY + 2, GR_PLANE = GR_PX * GR_PY;  // 340

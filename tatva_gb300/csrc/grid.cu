@@ -525,6 +525,20 @@ static void grid_coefficients(const double h[3], double mu, double lam, GridCoef
     }
 }
 
+// SMs of the current device (queried once per device).
+static int grid_sm_count() {
+  static int cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cached[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    cached[dev] = n;
+  }
+  return cached[dev];
+}
+
 // Coefficients and tiling of a structured-brick plan; returns the launch's CTA count
 // (boundary CTAs first, then the interior tiles), or -1 when it does not fit an int.
 template <class T>
@@ -537,7 +551,16 @@ static int64_t grid_setup(const tg_block_plan* plan, double mu, double lam, Grid
   const int ix = nx - 2, iy = ny - 2, iz = nz - 2;
   P.tiles_x = ix > 0 ? (ix + GR_TX - 1) / GR_TX : 0;
   P.tiles_y = iy > 0 ? (iy + GR_TY - 1) / GR_TY : 0;
+  // planes per tile: TG_GRID_TZ on large grids; fewer on small ones, so that the
+  // interior still spreads over about two CTAs per SM (a tile sweeps its planes one
+  // after the other, which sets the latency of a small grid's HVP)
   P.tz = TG_GRID_TZ;
+  if (iz > 0 && P.tiles_x > 0 && P.tiles_y > 0) {
+    const int64_t columns = (int64_t)P.tiles_x * P.tiles_y;
+    const int64_t want = 2 * (int64_t)grid_sm_count();
+    const int64_t tz = (columns * iz + want - 1) / want;
+    P.tz = (int)(tz < 2 ? 2 : (tz > TG_GRID_TZ ? TG_GRID_TZ : tz));
+  }
   P.tiles_z = iz > 0 ? (iz + P.tz - 1) / P.tz : 0;
   const int64_t n_int = (int64_t)P.tiles_x * P.tiles_y * P.tiles_z;
   P.n_boundary = (int64_t)nx * ny * nz - (int64_t)(ix > 0 ? ix : 0) * (iy > 0 ? iy : 0) *

@@ -601,6 +601,23 @@ struct CgBuffers {
   double *part, *scal;
   unsigned* ticket;  // [2] last-CTA arrival counters of the p.q and update kernels
   size_t apply_bytes;
+  // the captured run of check_every iterations: its buffers and operator are the same
+  // for every restart of one solve, so it is instantiated once per solve call (the
+  // caller destroys it with cg_release)
+  cudaGraphExec_t exec = nullptr;
+  int graph_len = 0;
+};
+
+static void cg_release(CgBuffers& B) {
+  if (B.exec) cudaGraphExecDestroy(B.exec);
+  B.exec = nullptr;
+  B.graph_len = 0;
+}
+
+// releases the solve's CUDA graph on every return path of a solve entry point
+struct CgGraphGuard {
+  CgBuffers& b;
+  ~CgGraphGuard() { cg_release(b); }
 };
 
 // The operator is linear elasticity on a structured brick whose plan carries the grid:
@@ -700,8 +717,8 @@ static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag
   if (!std::isfinite(h[SCAL_RR])) return set_error(TG_ERR_BREAKDOWN, "cg: non-finite residual");
   if (std::sqrt(h[SCAL_RR]) <= tol_abs) return TG_OK;
   check_every = check_every < 1 ? 1 : check_every;
-  cudaGraphExec_t exec = nullptr;
-  int graph_len = 0;
+  cudaGraphExec_t& exec = B.exec;
+  int& graph_len = B.graph_len;
   const bool can_capture = (st != nullptr) && (st != cudaStreamLegacy) && (st != cudaStreamPerThread);
   int rc = TG_OK;
   while (*iters < max_iter) {
@@ -738,7 +755,6 @@ static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag
     }
     if (std::sqrt(h[SCAL_RR]) <= tol_abs) break;
   }
-  if (exec) cudaGraphExecDestroy(exec);
   if (rc != TG_OK) return rc;
   if (std::sqrt(h[SCAL_RR]) > tol_abs)
     return set_error(TG_ERR_NOT_CONVERGED, "cg: not converged in %d iterations", *iters);
@@ -782,6 +798,7 @@ extern "C" int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, c
   if (!(rtol > 0.0) || max_iter < 0) return set_error(TG_ERR_VALUE, "bad rtol / max_iter");
   cudaStream_t st = as_stream(stream);
   CgBuffers B = cg_carve(op, workspace);
+  CgGraphGuard guard{B};
   return dispatch_prec(op->prec, [&](auto t) -> int {
     using T = decltype(t);
     double rn = 0, bn = 0;
@@ -838,6 +855,7 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
   cudaStream_t st = as_stream(stream);
   Carve c{(char*)workspace};
   CgBuffers B = cg_carve(op32, c.take(cg_bytes(op32)));
+  CgGraphGuard guard{B};
   const size_t ab64 = tg_operator_workspace_bytes(op64);
   void* aws64 = c.take(ab64);
   double* r64 = (double*)c.take(n * sizeof(double));

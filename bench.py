@@ -877,7 +877,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched", type=int, default=4096, help="meshes in the batched solve (0: skip)")
     ap.add_argument("--serving", type=int, default=200, help="requests in the serving run (0: skip)")
-    ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--newton", type=int, default=96, help="Kuhn cells per side (0: skip)")
     ap.add_argument("--newton-steps", type=int, default=10)
     ap.add_argument("--hbm-budget", type=int, default=32, help="serving HBM budget, GiB")

@@ -104,7 +104,7 @@ class BrickModel:
 
 
 class Server:
-    def __init__(self, device=None, slots: int = 8, hbm_budget: int = 16 << 30,
+    def __init__(self, device=None, slots: int = 16, hbm_budget: int = 16 << 30,
                  rtol: float = 1e-10, inner_rtol: float = 1e-4, check_every: int = 50,
                  max_outer: int = 50, max_inner: int = 200000, keep_solutions: bool = False):
         self.device = torch.device(device or "cuda")

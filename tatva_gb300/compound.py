@@ -246,6 +246,104 @@ class Compound:
         return self.arr
 
 
+class CompoundEnergy:
+    """Energy of a Compound state as a sum over its fields, E(s) = sum_f E_f(s.f), each
+    term one of the fused energies (``materials.Poisson / LinearElastic / NeoHookean``)
+    on an Operator over the compound's mesh.
+
+    The reference writes such energies as user JAX code over the fields of a state
+    (tatva/compound/__init__.py:73-300) and differentiates them with jax.grad / jax.jvp /
+    tatva.sparse.jacfwd on the pattern of ``pattern_from_compound``.  Here each field's
+    values are gathered from the flat state on the device through the field's index map,
+    the field's energy kernels compute its residual, HVP or compressed Hessian, and the
+    result is scattered back to the field's flat indices.  Only full nodal fields (one
+    row per mesh node, columns = the energy's components) can carry an energy; fields
+    without one contribute nothing (their rows are zero)."""
+
+    def __init__(self, compound_cls, **energies):
+        self.compound_cls = compound_cls
+        fields = dict(compound_cls.fields)
+        self.terms = []
+        for name, en in energies.items():
+            if name not in fields:
+                raise CompoundError(f"Unknown field name: {name}")
+            f = fields[name]
+            n_nodes = en.op.n_nodes
+            if not (isinstance(f.field_type, Nodal) and f.field_type.node_ids is None
+                    and f.shape[0] == n_nodes and int(prod(f.shape)) == en.n_dofs):
+                raise CompoundError(
+                    f"field '{name}' of shape {f.shape} is not a full nodal field with the "
+                    f"{en.n_values} components per node of its energy")
+            self.terms.append((name, f, en))
+        self._idx: dict = {}
+
+    @property
+    def n_dofs(self) -> int:
+        return self.compound_cls.size
+
+    def _index(self, f, device) -> torch.Tensor:
+        key = (f.name, str(device))
+        if key not in self._idx:
+            self._idx[key] = torch.as_tensor(f.indices(), device=device)
+        return self._idx[key]
+
+    def _flat(self, s):
+        arr = s.arr if isinstance(s, Compound) else s
+        if arr.numel() != self.n_dofs:
+            raise CompoundError(f"Array size {arr.numel()} does not match expected size "
+                                f"{self.n_dofs}.")
+        return arr.reshape(-1)
+
+    def _apply(self, method: str, s, v=None, fixed=None) -> torch.Tensor:
+        u = self._flat(s)
+        vv = self._flat(v) if v is not None else None
+        ref = u if u is not None else vv
+        out = torch.zeros(self.n_dofs, dtype=ref.dtype, device=ref.device)
+        for _, f, en in self.terms:
+            idx = self._index(f, ref.device)
+            mask = fixed[idx].contiguous() if fixed is not None else None
+            uf = u[idx].contiguous()
+            if method == "residual":
+                y = en.residual(uf, fixed=mask)
+            elif method == "hvp":
+                y = en.hvp(uf, vv[idx].contiguous(), fixed=mask)
+            else:
+                y = en.diagonal(uf, fixed=mask)
+            out[idx] = y.reshape(-1)
+        return out
+
+    def residual(self, s, fixed=None) -> torch.Tensor:
+        """dE/ds (jax.grad of the summed field energies), flat, in the compound layout."""
+        return self._apply("residual", s, fixed=fixed)
+
+    def hvp(self, s, v, fixed=None) -> torch.Tensor:
+        """d2E/ds2 . v (jax.jvp(jax.grad(E))), flat, in the compound layout."""
+        return self._apply("hvp", s, v, fixed=fixed)
+
+    def diagonal(self, s, fixed=None) -> torch.Tensor:
+        return self._apply("diagonal", s, fixed=fixed)
+
+    def value(self, s) -> torch.Tensor:
+        u = self._flat(s)
+        return sum(en.value(u[self._index(f, u.device)].contiguous()) for _, f, en in self.terms)
+
+    __call__ = value
+
+    def compressed_hessian(self, s, colors: torch.Tensor, n_colors: int,
+                           dtype=None) -> torch.Tensor:
+        """Jc (size, n_colors) on a distance-2 colouring of the compound pattern: each
+        field's rows from its energy's compressed Hessian with the colours of its own
+        columns (the energy couples no two fields, so the other columns add nothing)."""
+        u = self._flat(s)
+        dtype = dtype or u.dtype
+        Jc = torch.zeros((self.n_dofs, n_colors), dtype=dtype, device=u.device)
+        for _, f, en in self.terms:
+            idx = self._index(f, u.device)
+            Jc[idx] = en.compressed_hessian(u[idx].contiguous(), colors[idx].contiguous(),
+                                            n_colors, dtype=dtype)
+        return Jc
+
+
 def stack_fields(*names: str, axis: int = -1):
     """Class decorator: lay the named fields out as one block stacked along their last
     axis, starting where the first of them started; later fields follow the block."""
@@ -342,5 +440,6 @@ def pattern_from_compound(compound_cls, block_wise: bool = False):
     return [[full[a0:a1, b0:b1] for (b0, b1) in roots] for (a0, a1) in roots]
 
 
-__all__ = ["Compound", "CompoundError", "CompoundStackError", "Field", "FieldSize", "FieldType",
+__all__ = ["Compound", "CompoundEnergy", "CompoundError", "CompoundStackError", "Field", "FieldSize",
+           "FieldType",
            "Local", "Nodal", "Shared", "field", "pattern_from_compound", "stack_fields"]

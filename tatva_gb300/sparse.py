@@ -134,12 +134,13 @@ def decompress(Jc: torch.Tensor, rows: torch.Tensor, col_colors: torch.Tensor) -
 
 
 def _fused_energy(fn):
+    from .compound import CompoundEnergy
     from .materials import Energy
 
-    if isinstance(fn, Energy):
+    if isinstance(fn, (Energy, CompoundEnergy)):
         return fn
     owner = getattr(fn, "__self__", None)
-    if isinstance(owner, Energy) and getattr(fn, "__name__", "") == "residual":
+    if isinstance(owner, (Energy, CompoundEnergy)) and getattr(fn, "__name__", "") == "residual":
         return owner
     return None
 

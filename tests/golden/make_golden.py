@@ -3,6 +3,7 @@
 Run from the repository root, in a container that has the reference tree:
 
     python tests/golden/make_golden.py /path/to/reference
+    python tests/golden/make_golden.py /path/to/reference compound   # compound_golden.npz
 
 JAX is not installed where this runs, so a minimal numpy stand-in for the
 handful of ``jax`` entry points the reference modules touch at import time
@@ -362,5 +363,55 @@ def make(ref_root):
     print(f"wrote {len(out)} arrays to {os.path.join(HERE, 'reference_golden.npz')}")
 
 
+def make_compound(ref_root):
+    """Compound layouts and pattern_from_compound of the reference
+    (tatva/compound/__init__.py, tatva/sparse/_extraction.py:117-245) for three states on
+    small meshes; written to tests/golden/compound_golden.npz."""
+    ref = load_reference(ref_root)
+    import warnings
+
+    from tatva import compound as C
+
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle import mesh as om
+
+    out = {}
+    ct, et = om.kuhn_box((1, 1, 1), (2, 2, 1), origin=(0, 0, 0))
+    mt = ref.Mesh(ct, et)
+    cq, eq = om.unit_square(3, 2)
+    mq = ref.Mesh(cq, eq)
+
+    class TwoNodal(C.Compound, mesh=mt):
+        u = C.field((C.FieldSize.AUTO, 3))
+        theta = C.field((C.FieldSize.AUTO,))
+
+    class NodalAndLocal(C.Compound, mesh=mt):
+        u = C.field((C.FieldSize.AUTO, 3))
+        p = C.field((5,))
+
+    class PartialNodal(C.Compound, mesh=mq):
+        u = C.field((C.FieldSize.AUTO, 2))
+        lam = C.field((4,), field_type=C.field_types.Nodal(node_ids=np.array([0, 3, 5, 11])))
+
+    for name, cls in (("two_nodal", TwoNodal), ("nodal_local", NodalAndLocal),
+                      ("partial_nodal", PartialNodal)):
+        out[f"{name}_size"] = np.array(cls.size)
+        for fname, f in cls.fields:
+            out[f"{name}_field_{fname}"] = np.asarray(f.indices(slice(None))).reshape(-1)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            pat = ref.extraction.pattern_from_compound(cls)
+            blocks = ref.extraction.pattern_from_compound(cls, block_wise=True)
+        out[f"{name}_indptr"] = pat.indptr.astype(np.int64)
+        out[f"{name}_indices"] = pat.indices.astype(np.int64)
+        out[f"{name}_block_shapes"] = np.array([[b.shape[0], b.shape[1], b.nnz]
+                                                for row in blocks for b in row])
+    np.savez_compressed(os.path.join(HERE, "compound_golden.npz"), **out)
+    print("wrote", os.path.join(HERE, "compound_golden.npz"), len(out), "arrays")
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "compound":
+        make_compound(sys.argv[1])
+        sys.exit(0)
     make(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -120,3 +120,50 @@ def test_pattern_mixed_fields_and_blocks():
     with pytest.warns(UserWarning):
         blocks = pattern_from_compound(S, block_wise=True)
     assert len(blocks) == 2 and blocks[0][0].shape == (3 * N, 3 * N) and blocks[1][1].shape == (3, 3)
+
+
+def _golden_classes():
+    from tatva_gb300.compound import Nodal
+
+    ct, et = om.kuhn_box((1, 1, 1), (2, 2, 1), origin=(0, 0, 0))
+    mt = Mesh(ct, et, device="cpu")
+    cq, eq = om.unit_square(3, 2)
+    mq = Mesh(cq, eq, device="cpu")
+
+    class TwoNodal(Compound, mesh=mt):
+        u = field((FieldSize.AUTO, 3))
+        theta = field((FieldSize.AUTO,))
+
+    class NodalAndLocal(Compound, mesh=mt):
+        u = field((FieldSize.AUTO, 3))
+        p = field((5,))
+
+    class PartialNodal(Compound, mesh=mq):
+        u = field((FieldSize.AUTO, 2))
+        lam = field((4,), field_type=Nodal(node_ids=np.array([0, 3, 5, 11])))
+
+    return {"two_nodal": TwoNodal, "nodal_local": NodalAndLocal, "partial_nodal": PartialNodal}
+
+
+@pytest.mark.parametrize("name", ["two_nodal", "nodal_local", "partial_nodal"])
+def test_layout_and_pattern_bit_exact_vs_reference(name):
+    """Field index maps, pattern_from_compound and its block-wise split equal the
+    reference's own (tests/golden/compound_golden.npz, written by make_golden.py from
+    tatva/compound/__init__.py and tatva/sparse/_extraction.py:117-245)."""
+    import os
+    import warnings
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "compound_golden.npz"))
+    cls = _golden_classes()[name]
+    assert cls.size == int(g[f"{name}_size"])
+    for fname, f in cls.fields:
+        assert np.array_equal(np.asarray(f.indices(slice(None))).reshape(-1),
+                              g[f"{name}_field_{fname}"]), fname
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        pat = pattern_from_compound(cls)
+        blocks = pattern_from_compound(cls, block_wise=True)
+    assert np.array_equal(pat.indptr, g[f"{name}_indptr"])
+    assert np.array_equal(pat.indices, g[f"{name}_indices"])
+    shapes = np.array([[b.shape[0], b.shape[1], b.nnz] for row in blocks for b in row])
+    assert np.array_equal(shapes, g[f"{name}_block_shapes"])

@@ -544,6 +544,8 @@ def run_ours(args):
     }
     if tune:
         line["autotune"] = tune
+    if args.kernels:
+        line["maps"] = bench_maps(P, dev)
     if args.batched:
         line["batched"] = bench_batched(dev, args)
     if args.serving:
@@ -554,6 +556,98 @@ def run_ours(args):
 
 
 # ----------------------------------------------------------------------------- extras
+def _time_ms(fn, reps=5, warm=2):
+    """Mean CUDA-event time (ms) of fn() on the current stream, after warm-up calls."""
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def _roofline(nbytes, ms, what):
+    peak, kind = _peaks()
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    return {"ms": ms, "algorithmic_bytes": int(nbytes), "achieved_gbs": gbs, "peak_gbs": peak,
+            "frac": gbs / peak, "peak_source": kind, "bytes": what}
+
+
+def bench_maps(P, dev):
+    """Operator.grad and its transpose (the reverse-mode gather / scatter of
+    tatva/operator.py:194-223, 379-397) in FP64 on the 128^3 brick: every (element,
+    quadrature point) gradient materialised, as the reference does."""
+    import torch
+
+    op = P["op"]
+    E, N = P["n_elems"], P["n_nodes"]
+    u = torch.randn((N, 3), dtype=torch.float64, device=dev)
+    g = op._grad_raw(u)
+    out = {}
+    ms = _time_ms(lambda: op._grad_raw(u))
+    out["grad_f64"] = _roofline(4 * 8 * E + 8 * 3 * N * 2 + 8 * 72 * E, ms,
+                                "int32 connectivity, FP64 coordinates and nodal values in, "
+                                "FP64 (E, 8, 3, 3) gradients out")
+    ms = _time_ms(lambda: op._grad_t_raw(g, (3,)))
+    out["grad_transpose_f64"] = _roofline(8 * 72 * E + 4 * 8 * E + 8 * 3 * N * 2 + 4 * (N + 1 + 8 * E),
+                                          ms, "FP64 (E, 8, 3, 3) flux, connectivity, coordinates and "
+                                              "node incidence in, FP64 nodal values out")
+    del g
+    return out
+
+
+def bench_c3_kernels(P, en, cm, dev):
+    """The Neo-Hookean configuration's kernels at Kuhn 96^3: the general-path FP32 HVP,
+    the FP32 colored compressed Hessian (sparse/base.py:230-270), its decompression
+    (base.py:173) and the node-block SpMV of the CG on the tangent."""
+    import torch
+
+    from tatva_gb300 import _lib, sparse, solvers
+    from tatva_gb300._device import ptr, stream
+
+    N, E = P["n_nodes"], P["n_elems"]
+    nd = en.n_dofs
+    g = torch.Generator(device=dev).manual_seed(3)
+    u = (1e-3 * torch.randn(nd, generator=g, device=dev, dtype=torch.float64)).float()
+    v = torch.randn(nd, generator=g, device=dev, dtype=torch.float64).float()
+    out = {}
+    ms = _time_ms(lambda: en.hvp(u, v))
+    out["hvp_nh_f32"] = _roofline(3 * 4 * nd + 4 * 4 * E + 4 * 3 * N, ms,
+                                  "u and v read, y written (FP32), int32 connectivity, "
+                                  "FP32 coordinates")
+    C = cm.n_colors
+    ms = _time_ms(lambda: en.compressed_hessian(u, cm.colors, C), reps=3, warm=1)
+    out["compressed_hessian_f32"] = _roofline(4 * nd * C + 4 * nd + 4 * 4 * E + 4 * 3 * N + 4 * nd, ms,
+                                              "Jc (n_dofs x colours) written, u, colours, "
+                                              "connectivity, coordinates read")
+    Jc = en.compressed_hessian(u, cm.colors, C)
+    rows, cols = sparse.compute_rows_cols(cm)
+    ms = _time_ms(lambda: sparse.decompress(Jc, rows, cols), reps=3, warm=1)
+    out["decompress_f32"] = _roofline(16 * cm.nnz, ms, "rows, colour of the column, one Jc "
+                                                       "value read and one value written per entry")
+    del Jc, rows, cols
+    data = torch.randn(cm.nnz, generator=g, device=dev, dtype=torch.float32)
+    blocks = solvers.node_blocks3(cm)
+    y = torch.empty_like(v)
+    if blocks is not None:
+        nptr, nidx = blocks
+        ms = _time_ms(lambda: _lib.call("tg_spmv_blocks3", _lib.TG_F32, nd, ptr(cm.indptr),
+                                        ptr(nptr), ptr(nidx), ptr(data), ptr(v), ptr(y),
+                                        stream()))
+        out["spmv_blocks3_f32"] = _roofline(4 * cm.nnz + 4 * nidx.numel() + 4 * (nptr.numel() + nd + 1)
+                                            + 2 * 4 * nd, ms,
+                                            "FP32 values, one neighbour id per 3 x 3 block, "
+                                            "row and block pointers, x read and y written")
+    out["nnz"], out["n_colors"] = cm.nnz, C
+    return out
+
+
 BATCH_TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "batch_solve_poisson_4096.md")
 
 
@@ -753,6 +847,8 @@ def bench_newton(dev, args):
            "cg_iterations": cg_its, "nnz": cm.nnz, "n_colors": cm.n_colors,
            "converged_steps": sum(1 for h in hist if h["converged"]),
            "dof_newton_iterations_per_s": en.n_dofs * newton_its / total, "steps": hist}
+    if args.kernels:
+        out["kernels"] = bench_c3_kernels(P, en, cm, dev)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = _cpu_newton_sample()
     return out
@@ -807,7 +903,10 @@ def run_driver(args):
       Kuhn mesh with the linear-elastic law;
     * ``brick-cg``: ``--repeats`` Jacobi-CG iterations on the clamped brick;
     * ``batch``: the seeded random unit-square batch of ``--batched`` meshes, solved
-      ``--repeats`` times."""
+      ``--repeats`` times;
+    * ``kernels``: the map kernels on the brick of ``--size`` cells and the Neo-Hookean
+      kernels (HVP, compressed Hessian, decompression, node-block SpMV) on the Kuhn
+      block of ``--newton`` cells, as the bench's roofline legs run them."""
     import torch
 
     from tatva_gb300 import _lib, solvers
@@ -826,6 +925,17 @@ def run_driver(args):
             res = systems.solve(b)
         print(dict(info, converged=res.converged, max_rel_res=float(res.rel_res.max()),
                    seconds=res.seconds))
+        return
+    if name == "kernels":
+        from tatva_gb300 import sparse
+
+        Pb = clamped_brick(n, "cuda")
+        maps = bench_maps(Pb, torch.device("cuda"))
+        del Pb
+        Pk = stretched_kuhn(args.newton, "cuda")
+        cm = sparse.ColoredMatrix.from_csr(sparse.pattern_from_mesh(Pk["mesh"], 3), device="cuda")
+        ker = bench_c3_kernels(Pk, Pk["energy"], cm, torch.device("cuda"))
+        print(json.dumps({"maps": maps, "kernels": ker}))
         return
     if name == "brick-cg":
         P = clamped_brick(n, "cuda")
@@ -881,6 +991,8 @@ def main():
     ap.add_argument("--newton", type=int, default=96, help="Kuhn cells per side (0: skip)")
     ap.add_argument("--newton-steps", type=int, default=10)
     ap.add_argument("--hbm-budget", type=int, default=32, help="serving HBM budget, GiB")
+    ap.add_argument("--kernels", type=int, default=1,
+                    help="time the map, Hessian and SpMV kernels beside the solve (0: skip)")
     ap.add_argument("--driver", default="", help="run a profiling workload driver instead")
     ap.add_argument("--repeats", type=int, default=3, help="driver repetitions")
     ap.add_argument("--prec", default="f32", choices=["f32", "f64"], help="driver precision")

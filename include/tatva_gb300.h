@@ -111,11 +111,15 @@ TG_API int tg_scatter_nodal(int prec, const void* vals, int64_t n_nodes, int n_v
  * reference gets them from XLA's transpose of the gather at operator.py:221).
  * out (N,V) = sum over incident (e,a) of sum_q sum_d dNdX[e,q,d,a] flux[e,q,:,d]
  * The node->(e*n_e+a) incidence CSR comes from tg_node_incidence (HOST) and fixes
- * the summation order: the result is deterministic.                            */
+ * the summation order: the result is deterministic.  tg_grad_transpose forms each
+ * element's contribution to its nodes once (workspace of
+ * tg_grad_transpose_workspace_bytes: n_elems * nodes_per_elem * n_vals values),
+ * then sums them per node in incidence order.                                   */
+TG_API size_t tg_grad_transpose_workspace_bytes(int elem, int prec, int64_t n_elems, int n_vals);
 TG_API int tg_grad_transpose(int elem, int prec, const void* flux, const void* coords,
                       int64_t n_nodes, int n_vals, const int32_t* conn, int64_t n_elems,
                       const int32_t* inc_ptr, const int32_t* inc_idx, void* out,
-                      void* stream);
+                      void* workspace, size_t workspace_bytes, void* stream);
 TG_API int tg_eval_transpose(int elem, int prec, const void* quad, int64_t n_nodes, int n_vals,
                       const int32_t* conn, int64_t n_elems, const int32_t* inc_ptr,
                       const int32_t* inc_idx, void* out, void* stream);

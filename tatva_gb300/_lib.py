@@ -151,7 +151,8 @@ SIGNATURES = {
     "tg_gather_nodal": (I, [I, P, L, I, P, L, I, P, P]),
     "tg_integrate_quad_transpose": (I, [I, P, P, L, I, I, P, P]),
     "tg_scatter_nodal": (I, [I, P, L, I, I, P, P, P, P]),
-    "tg_grad_transpose": (I, [I, I, P, P, L, I, P, L, P, P, P, P]),
+    "tg_grad_transpose_workspace_bytes": (S, [I, I, L, I]),
+    "tg_grad_transpose": (I, [I, I, P, P, L, I, P, L, P, P, P, P, S, P]),
     "tg_eval_transpose": (I, [I, I, P, L, I, P, L, P, P, P, P]),
     "tg_plan_build": (I, [I, P, L, L, P, I, I, I, POINTER(c_void_p)]),
     "tg_plan_sizes": (I, [P, P]),

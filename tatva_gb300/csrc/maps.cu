@@ -62,6 +62,33 @@ __global__ void grad_kernel(const T* __restrict__ nodal, const T* __restrict__ c
   T X[NN][D];
   int nid[NN];
   gather_coords<ET, T>(coords, conn, e, X, nid);
+  if (V <= 3) {  // the element's values loaded once, not once per quadrature point
+    T U[NN][3];
+#pragma unroll
+    for (int a = 0; a < NN; ++a)
+#pragma unroll
+      for (int v = 0; v < 3; ++v) U[a][v] = v < V ? nodal[(int64_t)nid[a] * V + v] : T(0);
+#pragma unroll
+    for (int q = 0; q < E::Q; ++q) {
+      T G[NN][D];
+      qp_geometry<ET, T>(q, X, G);
+      T* o = out + ((e * E::Q + q) * V) * D;
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        if (v >= V) break;
+        T g[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) g[d] = T(0);
+#pragma unroll
+        for (int a = 0; a < NN; ++a)
+#pragma unroll
+          for (int d = 0; d < D; ++d) g[d] += G[a][d] * U[a][v];
+#pragma unroll
+        for (int d = 0; d < D; ++d) o[v * D + d] = g[d];
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < E::Q; ++q) {
     T G[NN][D];
@@ -174,44 +201,68 @@ __global__ void gather_nodal_kernel(const T* __restrict__ nodal, int V,
 }
 
 // ------------------------------------------------------------------ transposes
+// Phase 1: element e's contribution to each of its nodes, c[e][a][v] = sum_q sum_d
+// dNdX[e,q,d,a] flux[e,q,v,d], with the geometry of each quadrature point formed once
+// (values in groups of up to 3 per pass, so that the sums stay in registers).
 template <int ET, class T>
-__global__ void grad_transpose_kernel(const T* __restrict__ flux, const T* __restrict__ coords,
-                                      int64_t n_nodes, int V, const int32_t* __restrict__ conn,
-                                      const int32_t* __restrict__ inc_ptr,
-                                      const int32_t* __restrict__ inc_idx, T* __restrict__ out) {
+__global__ void grad_transpose_elem_kernel(const T* __restrict__ flux, const T* __restrict__ coords,
+                                           int V, const int32_t* __restrict__ conn,
+                                           int64_t n_elems, T* __restrict__ contrib) {
   using E = Elem<ET>;
   constexpr int NN = E::NN, D = E::D;
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= n_nodes) return;
-  for (int v = 0; v < V; ++v) out[n * V + v] = T(0);
-  for (int k = inc_ptr[n]; k < inc_ptr[n + 1]; ++k) {
-    const int ea = inc_idx[k];
-    const int64_t e = ea / NN;
-    const int a = ea % NN;
-    T X[NN][D];
-    int nid[NN];
-    gather_coords<ET, T>(coords, conn, e, X, nid);
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  T X[NN][D];
+  int nid[NN];
+  gather_coords<ET, T>(coords, conn, e, X, nid);
+  for (int v0 = 0; v0 < V; v0 += 3) {
+    const int nv = (V - v0) < 3 ? (V - v0) : 3;
+    T c[NN][3];
+#pragma unroll
+    for (int a = 0; a < NN; ++a)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) c[a][k] = T(0);
 #pragma unroll
     for (int q = 0; q < E::Q; ++q) {
       T G[NN][D];
       qp_geometry<ET, T>(q, X, G);
-      T ga[D];
+      const T* f = flux + ((e * E::Q + q) * V + v0) * D;
 #pragma unroll
-      for (int d = 0; d < D; ++d) {
-        ga[d] = G[0][d];
+      for (int k = 0; k < 3; ++k) {
+        if (k >= nv) break;
+        T fk[D];
 #pragma unroll
-        for (int b = 1; b < NN; ++b)
-          if (b == a) ga[d] = G[b][d];
-      }
-      const T* f = flux + ((e * E::Q + q) * V) * D;
-      for (int v = 0; v < V; ++v) {
-        T s = T(0);
+        for (int d = 0; d < D; ++d) fk[d] = f[k * D + d];
 #pragma unroll
-        for (int d = 0; d < D; ++d) s += ga[d] * f[v * D + d];
-        out[n * V + v] += s;
+        for (int a = 0; a < NN; ++a) {
+          T s = G[a][0] * fk[0];
+#pragma unroll
+          for (int d = 1; d < D; ++d) s += G[a][d] * fk[d];
+          c[a][k] += s;
+        }
       }
     }
+#pragma unroll
+    for (int a = 0; a < NN; ++a)
+      for (int k = 0; k < nv; ++k) contrib[(e * NN + a) * V + v0 + k] = c[a][k];
   }
+}
+
+// Phase 2: out[n] = the contributions of node n's incident (element, corner) pairs, in
+// the order of the incidence CSR (increasing element): deterministic.
+template <class T>
+__global__ void grad_transpose_node_kernel(const T* __restrict__ contrib, int64_t n_nodes, int V,
+                                           const int32_t* __restrict__ inc_ptr,
+                                           const int32_t* __restrict__ inc_idx,
+                                           T* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes * V) return;
+  const int64_t n = i / V;
+  const int v = (int)(i - n * V);
+  T s = T(0);
+  for (int k = __ldg(inc_ptr + n); k < __ldg(inc_ptr + n + 1); ++k)
+    s += contrib[(int64_t)__ldg(inc_idx + k) * V + v];
+  out[i] = s;
 }
 
 template <int ET, class T>
@@ -411,12 +462,23 @@ extern "C" int tg_gather_nodal(int prec, const void* nodal, int64_t n_nodes, int
   });
 }
 
+extern "C" size_t tg_grad_transpose_workspace_bytes(int elem, int prec, int64_t n_elems,
+                                                    int n_vals) {
+  const int NN = elem == TG_TRI3 ? 3 : (elem == TG_TET4 ? 4 : 8);
+  if (n_elems <= 0 || n_vals <= 0) return 0;
+  return (size_t)n_elems * NN * n_vals * (prec == TG_F32 ? 4 : 8);
+}
+
 extern "C" int tg_grad_transpose(int elem, int prec, const void* flux, const void* coords,
                                  int64_t n_nodes, int n_vals, const int32_t* conn,
                                  int64_t n_elems, const int32_t* inc_ptr, const int32_t* inc_idx,
-                                 void* out, void* stream) {
+                                 void* out, void* workspace, size_t workspace_bytes,
+                                 void* stream) {
   TG_TRY(check_sizes(n_elems, n_nodes, n_vals));
   if (n_nodes == 0) return TG_OK;
+  if (workspace_bytes < tg_grad_transpose_workspace_bytes(elem, prec, n_elems, n_vals))
+    return set_error(TG_ERR_WORKSPACE, "tg_grad_transpose: workspace too small (%zu < %zu)",
+                     workspace_bytes, tg_grad_transpose_workspace_bytes(elem, prec, n_elems, n_vals));
   TG_TRY(check_ptr(coords, "coords"));
   TG_TRY(check_ptr(inc_ptr, "inc_ptr"));
   TG_TRY(check_ptr(out, "out"));
@@ -429,8 +491,12 @@ extern "C" int tg_grad_transpose(int elem, int prec, const void* flux, const voi
     constexpr int ET = decltype(et)::value;
     return dispatch_prec(prec, [&](auto t) -> int {
       using T = decltype(t);
-      grad_transpose_kernel<ET, T><<<grid_for(n_nodes, 128), 128, 0, as_stream(stream)>>>(
-          (const T*)flux, (const T*)coords, n_nodes, n_vals, conn, inc_ptr, inc_idx, (T*)out);
+      if (n_elems > 0)
+        grad_transpose_elem_kernel<ET, T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
+            (const T*)flux, (const T*)coords, n_vals, conn, n_elems, (T*)workspace);
+      grad_transpose_node_kernel<T><<<grid_for(n_nodes * n_vals, 256), 256, 0,
+                                      as_stream(stream)>>>((const T*)workspace, n_nodes, n_vals,
+                                                           inc_ptr, inc_idx, (T*)out);
       return launch_check("tg_grad_transpose");
     });
   });

@@ -203,9 +203,12 @@ class Operator:
         V = int(math.prod(vshape)) if vshape else 1
         out = torch.empty((self.n_nodes,) + tuple(vshape), dtype=flux.dtype, device=flux.device)
         ip, ii = self.incidence()
+        nb = _lib.lib().tg_grad_transpose_workspace_bytes(self.element.tg_id,
+                                                          prec_of(flux.dtype), self.n_elements, V)
+        ws = torch.empty(max(int(nb), 1), dtype=torch.uint8, device=flux.device)
         _lib.call("tg_grad_transpose", self.element.tg_id, prec_of(flux.dtype), ptr(flux),
                   ptr(self.coords_as(flux.dtype)), self.n_nodes, V, ptr(self.mesh.elements),
-                  self.n_elements, ptr(ip), ptr(ii), ptr(out), stream())
+                  self.n_elements, ptr(ip), ptr(ii), ptr(out), ptr(ws), nb, stream())
         return out
 
     def _eval_t_raw(self, q: torch.Tensor, vshape) -> torch.Tensor:

@@ -748,7 +748,8 @@ def bench_serving(dev, args):
     from tatva_gb300 import serving
 
     reqs = serving.synthetic_requests(args.serving, rate=2000.0, seed=0)
-    srv = serving.Server(dev, slots=args.slots, hbm_budget=args.hbm_budget << 30)
+    srv = serving.Server(dev, slots=args.slots, hbm_budget=args.hbm_budget << 30,
+                         step_iterations=args.step_iterations)
     rep = srv.run(reqs, realtime=True)
     out = {"workload": f"{len(reqs)} requests, Poisson arrivals mean 2000/s, Hex8 LE bricks "
                        "side in {16,24,32,48,64}, mixed precision to rel-res 1e-10"}
@@ -987,7 +988,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched", type=int, default=4096, help="meshes in the batched solve (0: skip)")
     ap.add_argument("--serving", type=int, default=200, help="requests in the serving run (0: skip)")
-    ap.add_argument("--slots", type=int, default=16)
+    ap.add_argument("--slots", type=int, default=64, help="serving: solves in flight (<= 64)")
+    ap.add_argument("--step-iterations", type=int, default=20,
+                    help="serving: CG steps of the batch between two polls")
     ap.add_argument("--newton", type=int, default=96, help="Kuhn cells per side (0: skip)")
     ap.add_argument("--newton-steps", type=int, default=10)
     ap.add_argument("--hbm-budget", type=int, default=32, help="serving HBM budget, GiB")

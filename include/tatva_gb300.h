@@ -435,6 +435,72 @@ TG_API int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_desc* 
                    void* stream);
 
 /* ============================================================================
+ * Continuous batching of structured-brick solves (request loop).  No reference
+ * counterpart: each request is the matrix-free solve of README.md:93 (FP32 grid
+ * HVP inner Jacobi-CG, FP64 refinement on the true residual, as tg_mixed_solve on
+ * a brick), and up to TG_BRICK_MAX_SLOTS of them advance together, one launch per
+ * CG step for all.  A request's result is bitwise the same alone and in any mix.
+ * ========================================================================== */
+#define TG_BRICK_MAX_SLOTS 64
+/* slot phases */
+#define TG_BRICK_FREE 0
+#define TG_BRICK_REFINE 1 /* FP64 residual / restart pending */
+#define TG_BRICK_RUN 2    /* inner FP32 CG running */
+#define TG_BRICK_DONE 3   /* converged: status TG_OK */
+#define TG_BRICK_FAILED 4 /* status TG_ERR_NOT_CONVERGED or TG_ERR_BREAKDOWN */
+
+/* A linear-elastic Hex8 brick of nodes[0] x nodes[1] x nodes[2] nodes, node id
+ * i + nx (j + ny k), corner order of tatva/element/base.py:478-491, spacings h,
+ * Lame parameters mu, lam.  b: FP64 right-hand side (3 dofs per node, interleaved);
+ * x: FP64 solution (written: zero at admission, then the iterate); fixed: one byte
+ * per dof, nonzero = Dirichlet (identity row, value 0), or NULL.  b, x and fixed
+ * stay owned by the caller and must live until the slot is polled DONE / FAILED;
+ * workspace: tg_brick_workspace_bytes(nodes) bytes, 256-byte aligned, likewise.
+ * Converges to ||b - A x|| <= rtol ||b||; each inner solve stops at relative
+ * residual inner_rtol or max_inner iterations; at most max_outer inner solves.   */
+typedef struct tg_brick_request {
+  int32_t nodes[3];
+  int32_t reserved;
+  double h[3];
+  double mu, lam;
+  const double* b;
+  double* x;
+  const uint8_t* fixed;
+  void* workspace;
+  size_t workspace_bytes;
+  double rtol, inner_rtol;
+  int32_t max_outer, max_inner;
+} tg_brick_request;
+
+typedef struct tg_brick_state {
+  int32_t phase;      /* TG_BRICK_* */
+  int32_t status;     /* TG_OK / TG_ERR_NOT_CONVERGED / TG_ERR_BREAKDOWN when finished */
+  int32_t iterations; /* inner CG iterations so far */
+  int32_t outer;      /* inner solves started */
+  double rel_res;     /* ||b - A x|| / ||b|| at the last refinement */
+} tg_brick_state;
+
+typedef struct tg_brick_batch tg_brick_batch;
+
+/* The batch belongs to the current device; create / destroy allocate and free its
+ * slot table (not hot calls).                                                   */
+TG_API int tg_brick_batch_create(tg_brick_batch** out);
+TG_API void tg_brick_batch_destroy(tg_brick_batch* batch);
+TG_API size_t tg_brick_workspace_bytes(const int32_t nodes[3]);
+/* Takes the lowest free slot (TG_ERR_VALUE when all are taken); the solve starts
+ * at the next tg_brick_step.  Stream-ordered: the slot is written after the work
+ * already queued on `stream`.                                                   */
+TG_API int tg_brick_admit(tg_brick_batch* batch, const tg_brick_request* req, void* stream,
+                          int* slot);
+/* Enqueues one step for every slot in use: the refinement launches, then
+ * `iterations` CG steps (three launches each).  Does not synchronize.          */
+TG_API int tg_brick_step(tg_brick_batch* batch, int iterations, void* stream);
+/* Synchronizes `stream` and writes the state of all TG_BRICK_MAX_SLOTS slots to
+ * out (n_out >= TG_BRICK_MAX_SLOTS); slots reported DONE or FAILED are released
+ * (reported once, FREE afterwards).                                             */
+TG_API int tg_brick_poll(tg_brick_batch* batch, tg_brick_state* out, int n_out, void* stream);
+
+/* ============================================================================
  * HOST setup (H1).  Replaces tatva/sparse/_extraction.py _create_sparse_structure
  * / pattern_from_mesh (:37-102), tatva_coloring.distance2_colors as restated by
  * tatva/sparse/_coloring.py (:27-48, :136-153, :270-283).

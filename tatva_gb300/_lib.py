@@ -94,6 +94,39 @@ class SolveStats(ctypes.Structure):
     ]
 
 
+class BrickRequest(ctypes.Structure):
+    _fields_ = [
+        ("nodes", c_int32 * 3),
+        ("reserved", c_int32),
+        ("h", c_double * 3),
+        ("mu", c_double),
+        ("lam", c_double),
+        ("b", c_void_p),
+        ("x", c_void_p),
+        ("fixed", c_void_p),
+        ("workspace", c_void_p),
+        ("workspace_bytes", c_size_t),
+        ("rtol", c_double),
+        ("inner_rtol", c_double),
+        ("max_outer", c_int32),
+        ("max_inner", c_int32),
+    ]
+
+
+class BrickState(ctypes.Structure):
+    _fields_ = [
+        ("phase", c_int32),
+        ("status", c_int32),
+        ("iterations", c_int32),
+        ("outer", c_int32),
+        ("rel_res", c_double),
+    ]
+
+
+TG_BRICK_MAX_SLOTS = 64
+TG_BRICK_FREE, TG_BRICK_REFINE, TG_BRICK_RUN, TG_BRICK_DONE, TG_BRICK_FAILED = 0, 1, 2, 3, 4
+
+
 class BatchDesc(ctypes.Structure):
     _fields_ = [
         ("n_systems", c_int32),
@@ -184,6 +217,12 @@ SIGNATURES = {
     "tg_cg_solve": (I, [P, P, P, P, D, I, I, P, S, P, P]),
     "tg_mixed_workspace_bytes": (S, [P, P]),
     "tg_mixed_solve": (I, [P, P, P, P, P, D, D, I, I, I, P, S, P, P]),
+    "tg_brick_batch_create": (I, [POINTER(c_void_p)]),
+    "tg_brick_batch_destroy": (None, [P]),
+    "tg_brick_workspace_bytes": (S, [P]),
+    "tg_brick_admit": (I, [P, P, P, P]),
+    "tg_brick_step": (I, [P, I, P]),
+    "tg_brick_poll": (I, [P, P, I, P]),
     "tg_batch_ell_from_csr": (I, [P, L, P, P, P, P, P]),
     "tg_batch_workspace_bytes": (S, [L]),
     "tg_batch_solve": (I, [P, L, P, P, D, D, I, I, I, I, P, S, P, P, P, P, P]),

@@ -222,29 +222,33 @@ __global__ void grad_transpose_elem_kernel(const T* __restrict__ flux, const T* 
     for (int a = 0; a < NN; ++a)
 #pragma unroll
       for (int k = 0; k < 3; ++k) c[a][k] = T(0);
-#pragma unroll
+    // Not unrolled: the Hex8 geometry of eight points at once does not fit in registers.
+#pragma unroll 1
     for (int q = 0; q < E::Q; ++q) {
       T G[NN][D];
       qp_geometry<ET, T>(q, X, G);
       const T* f = flux + ((e * E::Q + q) * V + v0) * D;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        if (k >= nv) break;
-        T fk[D];
+        if (k < nv) {
+          T fk[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d) fk[d] = f[k * D + d];
+          for (int d = 0; d < D; ++d) fk[d] = f[k * D + d];
 #pragma unroll
-        for (int a = 0; a < NN; ++a) {
-          T s = G[a][0] * fk[0];
+          for (int a = 0; a < NN; ++a) {
+            T s = G[a][0] * fk[0];
 #pragma unroll
-          for (int d = 1; d < D; ++d) s += G[a][d] * fk[d];
-          c[a][k] += s;
+            for (int d = 1; d < D; ++d) s += G[a][d] * fk[d];
+            c[a][k] += s;
+          }
         }
       }
     }
 #pragma unroll
     for (int a = 0; a < NN; ++a)
-      for (int k = 0; k < nv; ++k) contrib[(e * NN + a) * V + v0 + k] = c[a][k];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (k < nv) contrib[(e * NN + a) * V + v0 + k] = c[a][k];
   }
 }
 

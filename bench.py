@@ -905,6 +905,8 @@ def run_driver(args):
     * ``brick-cg``: ``--repeats`` Jacobi-CG iterations on the clamped brick;
     * ``batch``: the seeded random unit-square batch of ``--batched`` meshes, solved
       ``--repeats`` times;
+    * ``serve``: ``--slots`` requests of the seeded serving mix admitted into one brick
+      batch, then ``--repeats`` steps of ``--step-iterations`` CG steps (all in flight);
     * ``kernels``: the map kernels on the brick of ``--size`` cells and the Neo-Hookean
       kernels (HVP, compressed Hessian, decompression, node-block SpMV) on the Kuhn
       block of ``--newton`` cells, as the bench's roofline legs run them."""
@@ -937,6 +939,35 @@ def run_driver(args):
         cm = sparse.ColoredMatrix.from_csr(sparse.pattern_from_mesh(Pk["mesh"], 3), device="cuda")
         ker = bench_c3_kernels(Pk, Pk["energy"], cm, torch.device("cuda"))
         print(json.dumps({"maps": maps, "kernels": ker}))
+        return
+    if name == "serve":
+        from tatva_gb300 import serving
+
+        srv = serving.Server("cuda", slots=args.slots, hbm_budget=64 << 30,
+                             step_iterations=args.step_iterations)
+        reqs = serving.synthetic_requests(args.slots, seed=0)
+        keep = []
+        st = srv.stream
+        with torch.cuda.stream(st):
+            for rq in reqs:
+                srv.model(rq.side)
+                r, t = srv._request(rq)
+                srv.batch.admit(r, st)
+                keep.append(t)
+            srv.batch.step(args.step_iterations, st)  # admission, first refinement, warm-up
+            srv.batch.poll(st)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                srv.batch.step(args.step_iterations, st)
+            states = srv.batch.poll(st)
+            dt = time.perf_counter() - t0
+        dofs = sum(srv.models[r.side].n_dofs for r in reqs)
+        running = sum(1 for s in states if s.phase == _lib.TG_BRICK_RUN)
+        its = reps * args.step_iterations
+        print(json.dumps({"driver": "serve", "requests": len(reqs), "dofs_in_flight": dofs,
+                          "running_at_end": running, "iterations": its,
+                          "us_per_iteration": 1e6 * dt / its,
+                          "ns_per_dof_iteration": 1e9 * dt / its / dofs}))
         return
     if name == "brick-cg":
         P = clamped_brick(n, "cuda")

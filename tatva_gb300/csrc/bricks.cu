@@ -431,7 +431,7 @@ int brick_chunks(int64_t n_dofs) {
 int64_t brick_grid_ctas(const int32_t nodes[3]) {
   GridCoef<float> P;
   const double h[3] = {1.0, 1.0, 1.0};
-  return grid_setup_dims<float>(nodes, h, 1.0, 1.0, P);
+  return grid_setup_dims<float>(nodes, h, 1.0, 1.0, P, true);
 }
 
 size_t brick_part_doubles(const int32_t nodes[3]) {
@@ -533,8 +533,8 @@ extern "C" int tg_brick_admit(tg_brick_batch* bt, const tg_brick_request* req, v
 
   BrickSlot h;
   std::memset(&h, 0, sizeof(h));
-  const int64_t g32 = grid_setup_dims<float>(nd, req->h, req->mu, req->lam, h.c32);
-  const int64_t g64 = grid_setup_dims<double>(nd, req->h, req->mu, req->lam, h.c64);
+  const int64_t g32 = grid_setup_dims<float>(nd, req->h, req->mu, req->lam, h.c32, true);
+  const int64_t g64 = grid_setup_dims<double>(nd, req->h, req->mu, req->lam, h.c64, true);
   if (g32 <= 0 || g64 != g32 || g32 > 0x3fffffff)
     return set_error(TG_ERR_VALUE, "tg_brick_admit: brick too large");
   h.n_nodes = (int64_t)nd[0] * nd[1] * nd[2];

@@ -510,9 +510,11 @@ static int grid_sm_count() {
 // Coefficients and tiling of a brick of nodes[0] x nodes[1] x nodes[2] nodes with
 // spacings h; returns the launch's CTA count (boundary CTAs first, then the interior
 // tiles), or -1 when it does not fit an int.
+// deep: always TG_GRID_TZ planes per tile (launches shared by many bricks need no
+// spreading of one brick over the SMs, and deeper tiles reload fewer halo planes).
 template <class T>
 static int64_t grid_setup_dims(const int32_t nodes[3], const double h[3], double mu, double lam,
-                               GridCoef<T>& P) {
+                               GridCoef<T>& P, bool deep = false) {
   const int nx = nodes[0], ny = nodes[1], nz = nodes[2];
   grid_coefficients<T>(h, mu, lam, P);
   P.nx = nx;
@@ -525,7 +527,7 @@ static int64_t grid_setup_dims(const int32_t nodes[3], const double h[3], double
   // interior still spreads over about two CTAs per SM (a tile sweeps its planes one
   // after the other, which sets the latency of a small grid's HVP)
   P.tz = TG_GRID_TZ;
-  if (iz > 0 && P.tiles_x > 0 && P.tiles_y > 0) {
+  if (!deep && iz > 0 && P.tiles_x > 0 && P.tiles_y > 0) {
     const int64_t columns = (int64_t)P.tiles_x * P.tiles_y;
     const int64_t want = 2 * (int64_t)grid_sm_count();
     const int64_t tz = (columns * iz + want - 1) / want;

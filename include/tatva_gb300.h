@@ -493,7 +493,9 @@ TG_API size_t tg_brick_workspace_bytes(const int32_t nodes[3]);
 TG_API int tg_brick_admit(tg_brick_batch* batch, const tg_brick_request* req, void* stream,
                           int* slot);
 /* Enqueues one step for every slot in use: the refinement launches, then
- * `iterations` CG steps (three launches each).  Does not synchronize.          */
+ * `iterations` CG steps (three launches each).  Does not synchronize.  The step is
+ * captured as a CUDA graph and replayed while the slots in use and `iterations`
+ * stay the same (a stream that cannot be captured gets plain launches).         */
 TG_API int tg_brick_step(tg_brick_batch* batch, int iterations, void* stream);
 /* Synchronizes `stream` and writes the state of all TG_BRICK_MAX_SLOTS slots to
  * out (n_out >= TG_BRICK_MAX_SLOTS); slots reported DONE or FAILED are released

@@ -456,6 +456,12 @@ struct tg_brick_batch {
   int grid_ctas[TG_BRICK_MAX_SLOTS] = {};
   int chunks[TG_BRICK_MAX_SLOTS] = {};
   std::vector<int> admitted;
+  // the last step's launches as a CUDA graph, replayed while the slots in use and the
+  // step length stay the same (a new admission or a release changes the tables)
+  cudaGraphExec_t exec = nullptr;
+  std::vector<int> exec_slots;
+  int exec_iterations = -1;
+  bool exec_stale = true;  // set by every admission (a slot may come back with another size)
 };
 
 extern "C" size_t tg_brick_workspace_bytes(const int32_t nodes[3]) {
@@ -492,6 +498,7 @@ extern "C" void tg_brick_batch_destroy(tg_brick_batch* bt) {
   if (bt->d_slots) cudaFree(bt->d_slots);
   if (bt->d_state) cudaFree(bt->d_state);
   if (bt->h_state) cudaFreeHost(bt->h_state);
+  if (bt->exec) cudaGraphExecDestroy(bt->exec);
   delete bt;
 }
 
@@ -576,6 +583,7 @@ extern "C" int tg_brick_admit(tg_brick_batch* bt, const tg_brick_request* req, v
   bt->grid_ctas[s] = h.grid_ctas;
   bt->chunks[s] = h.chunks;
   bt->admitted.push_back(s);
+  bt->exec_stale = true;
   *slot_out = s;
   return TG_OK;
 }
@@ -614,16 +622,56 @@ extern "C" int tg_brick_step(tg_brick_batch* bt, int iterations, void* stream) {
     const Launch La = make_launch(bt->admitted, bt->chunks, &na);
     brick_admit_kernel<<<(unsigned)na, 256, 0, st>>>(La, bt->d_slots);
     bt->admitted.clear();
+    TG_TRY(launch_check("tg_brick_step: admission"));
   }
-  brick_xupdate_kernel<<<(unsigned)nc, 256, 0, st>>>(Lc, bt->d_slots, bt->d_state);
-  brick_resid_kernel<<<(unsigned)ng, GR_THREADS, 0, st>>>(Lg, bt->d_slots, bt->d_state);
-  brick_restart_kernel<<<(unsigned)nc, DOT_THREADS, 0, st>>>(Lc, bt->d_slots, bt->d_state);
-  for (int it = 0; it < iterations; ++it) {
-    brick_hvp_kernel<<<(unsigned)ng, GR_THREADS, 0, st>>>(Lg, bt->d_slots, bt->d_state);
-    brick_update_kernel<<<(unsigned)nc, DOT_THREADS, 0, st>>>(Lc, bt->d_slots, bt->d_state);
-    brick_p_kernel<<<(unsigned)nc, DOT_THREADS, 0, st>>>(Lc, bt->d_slots, bt->d_state);
+  auto enqueue = [&]() {
+    brick_xupdate_kernel<<<(unsigned)nc, 256, 0, st>>>(Lc, bt->d_slots, bt->d_state);
+    brick_resid_kernel<<<(unsigned)ng, GR_THREADS, 0, st>>>(Lg, bt->d_slots, bt->d_state);
+    brick_restart_kernel<<<(unsigned)nc, DOT_THREADS, 0, st>>>(Lc, bt->d_slots, bt->d_state);
+    for (int it = 0; it < iterations; ++it) {
+      brick_hvp_kernel<<<(unsigned)ng, GR_THREADS, 0, st>>>(Lg, bt->d_slots, bt->d_state);
+      brick_update_kernel<<<(unsigned)nc, DOT_THREADS, 0, st>>>(Lc, bt->d_slots, bt->d_state);
+      brick_p_kernel<<<(unsigned)nc, DOT_THREADS, 0, st>>>(Lc, bt->d_slots, bt->d_state);
+    }
+  };
+  const bool can_capture = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+  if (!can_capture) {
+    enqueue();
+    return launch_check("tg_brick_step");
   }
-  return launch_check("tg_brick_step");
+  if (!bt->exec || bt->exec_stale || bt->exec_slots != active ||
+      bt->exec_iterations != iterations) {
+    cudaGraph_t graph;
+    TG_TRY(cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal),
+                      "brick step: capture"));
+    enqueue();
+    const cudaError_t le = cudaGetLastError();
+    const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    TG_TRY(cuda_check(le, "brick step: launches"));
+    TG_TRY(cuda_check(ee, "brick step: end capture"));
+    bool updated = false;
+    if (bt->exec) {  // same number of launches: update the parameters in place
+      cudaGraphExecUpdateResultInfo info;
+      updated = bt->exec_iterations == iterations &&
+                cudaGraphExecUpdate(bt->exec, graph, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(bt->exec);
+        bt->exec = nullptr;
+      }
+    }
+    int rc = TG_OK;
+    if (!updated) rc = cuda_check(cudaGraphInstantiate(&bt->exec, graph, 0), "brick step: instantiate");
+    cudaGraphDestroy(graph);
+    if (rc != TG_OK) {
+      bt->exec = nullptr;
+      return rc;
+    }
+    bt->exec_slots = active;
+    bt->exec_iterations = iterations;
+    bt->exec_stale = false;
+  }
+  return cuda_check(cudaGraphLaunch(bt->exec, st), "brick step: graph launch");
 }
 
 extern "C" int tg_brick_poll(tg_brick_batch* bt, tg_brick_state* out, int n_out, void* stream) {

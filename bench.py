@@ -903,6 +903,8 @@ def run_driver(args):
       clamped brick (``--size`` cells per side), the Neo-Hookean Kuhn block, or the same
       Kuhn mesh with the linear-elastic law;
     * ``brick-cg``: ``--repeats`` Jacobi-CG iterations on the clamped brick;
+    * ``mixed``: ``--repeats`` mixed-precision solves of the clamped brick to rel-res
+      1e-10 (the headline's solve);
     * ``batch``: the seeded random unit-square batch of ``--batched`` meshes, solved
       ``--repeats`` times;
     * ``serve``: ``--slots`` requests of the seeded serving mix admitted into one brick
@@ -969,6 +971,16 @@ def run_driver(args):
                           "us_per_iteration": 1e6 * dt / its,
                           "ns_per_dof_iteration": 1e9 * dt / its / dofs}))
         return
+    if name == "mixed":
+        P = clamped_brick(n, "cuda")
+        for _ in range(reps):
+            r = solvers.mixed_cg(P["energy"], P["b"], fixed=P["fixed"], rtol=RTOL,
+                                 inner_rtol=args.inner_rtol, check_every=args.check_every)
+        torch.cuda.synchronize()
+        print(json.dumps({"driver": "mixed", "dofs": P["energy"].n_dofs,
+                          "inner_iterations": r.iterations, "refinements": r.outer,
+                          "rel_res": r.rel_res}))
+        return
     if name == "brick-cg":
         P = clamped_brick(n, "cuda")
         bb = P["b"].to(dtype)
@@ -1018,7 +1030,7 @@ def main():
     ap.add_argument("--cpu-iterations", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched", type=int, default=4096, help="meshes in the batched solve (0: skip)")
-    ap.add_argument("--serving", type=int, default=200, help="requests in the serving run (0: skip)")
+    ap.add_argument("--serving", type=int, default=400, help="requests in the serving run (0: skip)")
     ap.add_argument("--slots", type=int, default=64, help="serving: solves in flight (<= 64)")
     ap.add_argument("--step-iterations", type=int, default=20,
                     help="serving: CG steps of the batch between two polls")

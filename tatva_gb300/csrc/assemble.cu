@@ -1032,7 +1032,8 @@ extern "C" int tg_apply(int elem, int prec, int mode, const tg_material* mat,
             if (n_aff < 0 || n_aff > plan->n_blocks)
               return set_error(TG_ERR_VALUE, "plan.n_affine_blocks out of range");
             if constexpr (ET == TG_HEX8 && MAT == TG_LINEAR_ELASTIC &&
-                          (MODE == TG_MODE_HVP || MODE == TG_MODE_RESIDUAL)) {
+                          (MODE == TG_MODE_HVP || MODE == TG_MODE_RESIDUAL ||
+                           MODE == TG_MODE_DIAG)) {
               // structured brick: the stencil schedule over the grid
               if (plan->grid_nodes[0] > 0 && mat->elem_param == nullptr &&
                   (int64_t)plan->grid_nodes[0] * plan->grid_nodes[1] * plan->grid_nodes[2] ==

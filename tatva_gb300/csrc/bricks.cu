@@ -257,13 +257,13 @@ __global__ void __launch_bounds__(DOT_THREADS)
   const int b = blockIdx.x - L.off[e], count = L.off[e + 1] - L.off[e];
   int64_t i0, i1;
   chunk_of(S->n_dofs, b, count, i0, i1);
-  const double sc = S->s;
+  const double inv_s = 1.0 / S->s;  // one division per thread, not per element
   const double* r64 = S->r64;
   float *r = S->r, *d = S->d, *p = S->p;
   const float* dinv = S->dinv;
   DotAcc<float> a0, a1;
   for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) {
-    const float ri = (float)(r64[i] / sc);
+    const float ri = (float)(r64[i] * inv_s);
     const float zi = ri * dinv[i];
     r[i] = ri;
     d[i] = 0.0f;

@@ -11,6 +11,31 @@ __global__ void pack_node_mask_kernel(const uint8_t* __restrict__ fixed, int64_t
   if (g < n_nodes) out[g] = (uint8_t)mask_bits<MASK_DOF>(fixed, g);
 }
 
+// Jacobi diagonal of the brick's operator: per dof, the sum of the element matrix's
+// diagonal entry over the cells that exist around the node (the element-by-element sum
+// of the reference's Hessian diagonal); fixed dofs get 1, the identity rows of the
+// Dirichlet-masked operator.
+template <class T>
+__global__ void grid_diag_kernel(const __grid_constant__ GridCoef<T> P,
+                                 const uint8_t* __restrict__ fixed, T* __restrict__ y) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t plane = (int64_t)P.nx * P.ny;
+  if (g >= plane * P.nz) return;
+  const int x = (int)(g % P.nx), yy = (int)((g / P.nx) % P.ny), z = (int)(g / plane);
+  const int bits = fixed ? mask_bits<MASK_DOF>(fixed, g) : 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    T sum = T(0);
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {  // cell whose corner o is this node
+      const int cx = x - (o & 1), cy = yy - ((o >> 1) & 1), cz = z - (o >> 2);
+      if (cx >= 0 && cy >= 0 && cz >= 0 && cx < P.nx - 1 && cy < P.ny - 1 && cz < P.nz - 1)
+        sum += P.ke[o][o][a][a];
+    }
+    y[3 * g + a] = (bits >> a & 1) ? T(1) : sum;
+  }
+}
+
 // Device scalars and partials of the CG dot that a DOT launch produces.
 struct GridDot {
   double* scal;    // SCAL_* slots: reads RZ and FLAG, writes PQ, ALPHA, FLAG
@@ -64,6 +89,11 @@ static int launch_grid_le_t(const tg_block_plan* plan, int mode, const T* u, con
   const int64_t n = grid_setup<T>(plan, mu, lam, P);
   if (n < 0) return set_error(TG_ERR_VALUE, "grid too large");
   if (n == 0) return TG_OK;
+  if (mode == TG_MODE_DIAG) {
+    const int64_t nn = (int64_t)P.nx * P.ny * P.nz;
+    grid_diag_kernel<T><<<grid_for(nn, 256), 256, 0, st>>>(P, fixed, y);
+    return launch_check("grid diagonal kernel");
+  }
   const T* in = (mode == TG_MODE_HVP) ? v : u;
   const unsigned grid = (unsigned)n;
   const GridDot D{nullptr, nullptr, nullptr};
@@ -117,7 +147,8 @@ int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double l
 
 int launch_grid_le(const tg_block_plan* plan, int prec, int mode, const void* u, const void* v,
                    const uint8_t* fixed, void* y, double mu, double lam, cudaStream_t st) {
-  if (mode != TG_MODE_HVP && mode != TG_MODE_RESIDUAL) return TG_ERR_UNSUPPORTED;
+  if (mode != TG_MODE_HVP && mode != TG_MODE_RESIDUAL && mode != TG_MODE_DIAG)
+    return TG_ERR_UNSUPPORTED;
   if (plan->grid_nodes[0] < 2 || plan->grid_nodes[1] < 2 || plan->grid_nodes[2] < 2)
     return TG_ERR_UNSUPPORTED;
   if (prec == TG_F32)

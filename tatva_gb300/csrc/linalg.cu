@@ -397,18 +397,20 @@ __global__ void cg_p_kernel(int64_t n, const double* __restrict__ scal, const T*
   }
 }
 
-// out = (T)(r64 / s) with s = sqrt(rr) read on the device
+// out = (T)(r64 / |r64|) and x += |r64| d, the scale and its reciprocal passed in
+// (an FP64 square root or division per element costs more than the memory traffic on
+// this GPU's FP64 pipe)
 template <class T>
-__global__ void scale_down_kernel(int64_t n, const double* __restrict__ r64,
-                                  const double* __restrict__ s2, T* __restrict__ out) {
+__global__ void scale_down_kernel(int64_t n, const double* __restrict__ r64, double inv_s,
+                                  T* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (T)(r64[i] / sqrt(s2[0]));
+  if (i < n) out[i] = (T)(r64[i] * inv_s);
 }
 template <class T>
-__global__ void scale_up_add_kernel(int64_t n, const T* __restrict__ d,
-                                    const double* __restrict__ s2, double* __restrict__ x) {
+__global__ void scale_up_add_kernel(int64_t n, const T* __restrict__ d, double s,
+                                    double* __restrict__ x) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] += sqrt(s2[0]) * (double)d[i];
+  if (i < n) x[i] += s * (double)d[i];
 }
 
 // ------------------------------------------------------------------ operator description
@@ -888,7 +890,7 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
     if (rn <= rtol * bn || bn == 0.0) break;
     if (outer >= max_outer) { rc = set_error(TG_ERR_NOT_CONVERGED, "mixed: not converged after %d refinements", outer); break; }
     // inner FP32 solve A32 d = r64 / |r64|, d0 = 0
-    scale_down_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, r64, sc, r32);
+    scale_down_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, r64, 1.0 / rn, r32);
     TG_TRY(cuda_check(cudaMemsetAsync(d32, 0, n * sizeof(float), st), "mixed: zero"));
     int it = 0;
     const int irc = cg_run<float>(op32, r32, d32, diag32, inner_rtol, max_inner, check_every, B, st, &it);
@@ -896,7 +898,7 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
     if (irc == TG_ERR_BREAKDOWN) { rc = irc; break; }
     if (irc != TG_OK && irc != TG_ERR_NOT_CONVERGED) { rc = irc; break; }
     // x += |r64| d
-    scale_up_add_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, d32, sc, x);
+    scale_up_add_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, d32, rn, x);
     TG_TRY(launch_check("mixed: update"));
     ++outer;
   }

@@ -145,3 +145,28 @@ def test_grid_cg_matches_element_cg_and_is_deterministic(cuda, check_every):
     ref = e1.x.cpu().numpy()
     for res in (r1, m1, em):
         assert rel(res.x, ref) < 1e-8
+
+
+def test_grid_diagonal_matches_element_blocks_and_oracle(cuda):
+    """Jacobi diagonal on the grid (per node, the element diagonal summed over the cells
+    around it; fixed dofs 1) against the element-block schedule and the oracle's sum
+    of element-tangent diagonals."""
+    c, e, en, v, u, fixed = _setup((7, 5, 6), (0.7, 0.5, 1.2), cuda)
+    f = torch.as_tensor(fixed, device=cuda)
+    ut = torch.zeros(en.n_dofs, dtype=torch.float64, device=cuda)
+    d_grid = en.diagonal(ut, f)
+    plan = en.plan()
+    plan.grid = False
+    try:
+        d_el = en.diagonal(ut, f)
+    finally:
+        plan.grid = True
+    assert rel(d_grid, d_el) < SWAP64_TOL
+    oo = oop.OracleOperator(c, e, oe.Hexahedron8())
+    Ke = omat.element_tangents(oo, omat.LinearElastic(MU, LAM), np.zeros(en.n_dofs))
+    dofs = (e[:, :, None] * 3 + np.arange(3)).reshape(e.shape[0], -1)
+    d = np.zeros(en.n_dofs)
+    np.add.at(d, dofs.ravel(), np.einsum("eii->ei", Ke).ravel())
+    d[fixed == 1] = 1.0
+    assert rel(d_grid, d) < F64_TOL
+    assert rel(en.diagonal(ut.float(), f), d) < F32_TOL

@@ -110,6 +110,212 @@ __global__ void grad_kernel(const T* __restrict__ nodal, const T* __restrict__ c
   }
 }
 
+// ------------------------------------------------------------------ Hex8 modal form
+// The trilinear map of a Hex8 cell is x(xi) = sum_m c_m xi^m over the eight monomials
+// m of {1, xi1, xi2, xi1 xi2, xi3, xi1 xi3, xi2 xi3, xi1 xi2 xi3} (bit k of m: factor
+// xi_{k+1}), with c_m = 1/8 sum_a (prod_{k in m} s_{a,k}) x_a for the corner signs
+// s_{a,k} of tatva/element/base.py:478-491.  Then
+//   dx/dxi1 = c_1 + c_3 xi2 + c_5 xi3 + c_7 xi2 xi3   (and cyclically),
+// so J at a quadrature point costs 3 FMAs per entry instead of an 8-term sum, and the
+// same transform of the nodal values gives their reference gradient.  The transform
+// is a 3-stage butterfly over the corners in binary order (reference node a is binary
+// corner {0,1,3,2,4,5,7,6}[a]).  GB300's FP64 pipe bounds these FP64 maps, so the
+// operation count is what sets their time.  A parallelepiped cell has c_3 = c_5 =
+// c_6 = c_7 = 0 exactly: its J is the same at every point and is inverted once
+// (bitwise what the per-point evaluation gives).
+__host__ __device__ constexpr int hex_bin(int a) { return a ^ ((a >> 1) & 1); }
+
+// corners (reference order) -> modes c_m, C components, in place
+template <class T, int C>
+__device__ __forceinline__ void hex_modes(T (&v)[8][C]) {
+  T w[8][C];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int c = 0; c < C; ++c) w[hex_bin(a)][c] = v[a][c];
+#pragma unroll
+  for (int k = 1; k < 8; k <<= 1)
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+      if (!(b & k))
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const T x = w[b][c], y = w[b | k][c];
+          w[b][c] = x + y;
+          w[b | k][c] = y - x;
+        }
+#pragma unroll
+  for (int m = 0; m < 8; ++m)
+#pragma unroll
+    for (int c = 0; c < C; ++c) v[m][c] = w[m][c] * T(0.125);
+}
+
+// adjoint of hex_modes: mode weights -> corner (reference order) contributions
+template <class T, int C>
+__device__ __forceinline__ void hex_modes_adjoint(T (&w)[8][C], T (&out)[8][C]) {
+#pragma unroll
+  for (int k = 1; k < 8; k <<= 1)
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+      if (!(b & k))
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const T x = w[b][c], y = w[b | k][c];
+          w[b][c] = x - y;
+          w[b | k][c] = x + y;
+        }
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int c = 0; c < C; ++c) out[a][c] = w[hex_bin(a)][c] * T(0.125);
+}
+
+// d/dxi_i of the modal field at xi: D[i][c]
+template <class T, int C>
+__device__ __forceinline__ void hex_dxi(const T (&m)[8][C], const T (&xi)[3], T (&D)[3][C]) {
+  const T x12 = xi[0] * xi[1], x13 = xi[0] * xi[2], x23 = xi[1] * xi[2];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    D[0][c] = fma(m[7][c], x23, fma(m[5][c], xi[2], fma(m[3][c], xi[1], m[1][c])));
+    D[1][c] = fma(m[7][c], x13, fma(m[6][c], xi[2], fma(m[3][c], xi[0], m[2][c])));
+    D[2][c] = fma(m[7][c], x12, fma(m[6][c], xi[1], fma(m[5][c], xi[0], m[4][c])));
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void hex_qp(int q, T (&xi)[3]) {
+  const T g = T(HEX_GAUSS);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) xi[i] = Elem<TG_HEX8>::s(q, i) > 0 ? g : -g;
+}
+
+template <class T>
+__device__ __forceinline__ bool hex_affine(const T (&mx)[8][3]) {
+  bool z = true;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    z = z && mx[3][c] == T(0) && mx[5][c] == T(0) && mx[6][c] == T(0) && mx[7][c] == T(0);
+  return z;
+}
+
+// out[e, q, v, d] = sum_i Ji[d][i] dU_v/dxi_i
+template <class T>
+__global__ void __launch_bounds__(128) hex_grad_kernel(const T* __restrict__ nodal,
+                                                       const T* __restrict__ coords, int V,
+                                                       const int32_t* __restrict__ conn,
+                                                       int64_t n_elems, T* __restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  T mx[8][3];
+  int nid[8];
+  gather_coords<TG_HEX8, T>(coords, conn, e, mx, nid);
+  hex_modes<T, 3>(mx);
+  const bool affine = hex_affine(mx);
+  T Ji[3][3];
+  if (affine) {
+    T xi[3] = {T(0), T(0), T(0)}, J[3][3];
+    hex_dxi<T, 3>(mx, xi, J);
+    inv3(J, Ji);
+  }
+  for (int v0 = 0; v0 < V; v0 += 3) {
+    const int nv = (V - v0) < 3 ? (V - v0) : 3;
+    T mu[8][3];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) mu[a][k] = k < nv ? nodal[(int64_t)nid[a] * V + v0 + k] : T(0);
+    hex_modes<T, 3>(mu);
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+      T xi[3];
+      hex_qp<T>(q, xi);
+      if (!affine) {
+        T J[3][3];
+        hex_dxi<T, 3>(mx, xi, J);
+        inv3(J, Ji);
+      }
+      T H[3][3];  // H[i][k] = dU_k/dxi_i
+      hex_dxi<T, 3>(mu, xi, H);
+      T* o = out + ((e * 8 + q) * V + v0) * 3;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k < nv) {
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            o[k * 3 + d] = fma(Ji[d][2], H[2][k], fma(Ji[d][1], H[1][k], Ji[d][0] * H[0][k]));
+        }
+      }
+    }
+  }
+}
+
+// contrib[e, a, v] = sum_q sum_d dN_a/dx_d flux[e, q, v, d]
+//                 = sum_q sum_i dN_a/dxi_i F_i,  F_i = sum_d Ji[d][i] flux[e, q, v, d],
+// accumulated in the modal basis and returned to the corners by the adjoint transform
+template <class T>
+__global__ void __launch_bounds__(128)
+    hex_grad_transpose_elem_kernel(const T* __restrict__ flux, const T* __restrict__ coords,
+                                   int V, const int32_t* __restrict__ conn, int64_t n_elems,
+                                   T* __restrict__ contrib) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_elems) return;
+  T mx[8][3];
+  int nid[8];
+  gather_coords<TG_HEX8, T>(coords, conn, e, mx, nid);
+  hex_modes<T, 3>(mx);
+  const bool affine = hex_affine(mx);
+  T Ji[3][3];
+  if (affine) {
+    T xi[3] = {T(0), T(0), T(0)}, J[3][3];
+    hex_dxi<T, 3>(mx, xi, J);
+    inv3(J, Ji);
+  }
+  for (int v0 = 0; v0 < V; v0 += 3) {
+    const int nv = (V - v0) < 3 ? (V - v0) : 3;
+    T w[8][3];
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) w[m][k] = T(0);
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+      T xi[3];
+      hex_qp<T>(q, xi);
+      if (!affine) {
+        T J[3][3];
+        hex_dxi<T, 3>(mx, xi, J);
+        inv3(J, Ji);
+      }
+      const T* f = flux + ((e * 8 + q) * V + v0) * 3;
+      const T x12 = xi[0] * xi[1], x13 = xi[0] * xi[2], x23 = xi[1] * xi[2];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k < nv) {
+          const T f0 = f[k * 3], f1 = f[k * 3 + 1], f2 = f[k * 3 + 2];
+          T F[3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) F[i] = fma(Ji[2][i], f2, fma(Ji[1][i], f1, Ji[0][i] * f0));
+          // adjoint of hex_dxi
+          w[1][k] += F[0];
+          w[2][k] += F[1];
+          w[4][k] += F[2];
+          w[3][k] = fma(F[0], xi[1], fma(F[1], xi[0], w[3][k]));
+          w[5][k] = fma(F[0], xi[2], fma(F[2], xi[0], w[5][k]));
+          w[6][k] = fma(F[1], xi[2], fma(F[2], xi[1], w[6][k]));
+          w[7][k] = fma(F[0], x23, fma(F[1], x13, fma(F[2], x12, w[7][k])));
+        }
+      }
+    }
+    T c[8][3];
+    hex_modes_adjoint<T, 3>(w, c);
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (k < nv) contrib[(e * 8 + a) * V + v0 + k] = c[a][k];
+  }
+}
+
 // ------------------------------------------------------------------ weights
 template <int ET, class T>
 __global__ void weights_kernel(const T* __restrict__ coords, const int32_t* __restrict__ conn,
@@ -384,8 +590,12 @@ extern "C" int tg_grad(int elem, int prec, const void* nodal, const void* coords
     constexpr int ET = decltype(et)::value;
     return dispatch_prec(prec, [&](auto t) -> int {
       using T = decltype(t);
-      grad_kernel<ET, T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
-          (const T*)nodal, (const T*)coords, n_vals, conn, n_elems, (T*)out);
+      if constexpr (ET == TG_HEX8)
+        hex_grad_kernel<T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
+            (const T*)nodal, (const T*)coords, n_vals, conn, n_elems, (T*)out);
+      else
+        grad_kernel<ET, T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
+            (const T*)nodal, (const T*)coords, n_vals, conn, n_elems, (T*)out);
       return launch_check("tg_grad");
     });
   });
@@ -495,9 +705,16 @@ extern "C" int tg_grad_transpose(int elem, int prec, const void* flux, const voi
     constexpr int ET = decltype(et)::value;
     return dispatch_prec(prec, [&](auto t) -> int {
       using T = decltype(t);
-      if (n_elems > 0)
-        grad_transpose_elem_kernel<ET, T><<<grid_for(n_elems, 128), 128, 0, as_stream(stream)>>>(
-            (const T*)flux, (const T*)coords, n_vals, conn, n_elems, (T*)workspace);
+      if (n_elems > 0) {
+        if constexpr (ET == TG_HEX8)
+          hex_grad_transpose_elem_kernel<T><<<grid_for(n_elems, 128), 128, 0,
+                                              as_stream(stream)>>>(
+              (const T*)flux, (const T*)coords, n_vals, conn, n_elems, (T*)workspace);
+        else
+          grad_transpose_elem_kernel<ET, T><<<grid_for(n_elems, 128), 128, 0,
+                                              as_stream(stream)>>>(
+              (const T*)flux, (const T*)coords, n_vals, conn, n_elems, (T*)workspace);
+      }
       grad_transpose_node_kernel<T><<<grid_for(n_nodes * n_vals, 256), 256, 0,
                                       as_stream(stream)>>>((const T*)workspace, n_nodes, n_vals,
                                                            inc_ptr, inc_idx, (T*)out);

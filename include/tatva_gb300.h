@@ -313,12 +313,14 @@ TG_API int tg_batch_solve(const tg_batch_desc* desc, int64_t n_rows, const doubl
 
 /* Jc (n_nodes*V, n_colors) row-major, overwritten:
  *   Jc[i, c] = sum_{j : dof_colors[j] == c} H[i, j],  H = d2E/du2(u)
- * computed from element tangents, accumulated in element-colour order
- * (elem_order/elem_color_ptr from tg_element_colors; elem_color_ptr is HOST). */
+ * computed from element tangents: each node's rows sum the row blocks of its
+ * incident (element, corner) pairs in the order of the incidence CSR inc_ptr /
+ * inc_idx (tg_node_incidence, device copies): deterministic.  Decompression
+ * (tg_decompress) needs dof_colors to be a distance-2 colouring (each colour at
+ * most once per row of the pattern).                                             */
 TG_API int tg_compressed_hessian(int elem, int prec, const tg_material* mat, const void* coords,
                           int64_t n_nodes, const int32_t* conn, int64_t n_elems,
-                          const void* u, const int32_t* elem_order,
-                          const int32_t* elem_color_ptr_host, int n_elem_colors,
+                          const void* u, const int32_t* inc_ptr, const int32_t* inc_idx,
                           const int32_t* dof_colors, int n_colors, void* Jc, void* stream);
 /* rows[k] = row of nonzero k; col_colors[k] = colors[indices[k]]   base.py:108-136 */
 TG_API int tg_rows_cols(const int32_t* indptr, const int32_t* indices, const int32_t* colors,

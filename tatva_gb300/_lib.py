@@ -197,7 +197,7 @@ SIGNATURES = {
     "tg_apply": (I, [I, I, I, P, P, P, L, P, P, P, P, P, S, P]),
     "tg_apply_noalloc": (I, [I, I, I, P, P, P, L, P, P, P, P, P]),
     "tg_energy_per_element": (I, [I, I, P, P, L, P, L, P, P, P]),
-    "tg_compressed_hessian": (I, [I, I, P, P, L, P, L, P, P, P, I, P, I, P, P]),
+    "tg_compressed_hessian": (I, [I, I, P, P, L, P, L, P, P, P, P, I, P, P]),
     "tg_rows_cols": (I, [P, P, P, L, L, P, P, P]),
     "tg_decompress": (I, [I, P, I, P, P, L, P, P]),
     "tg_color_seeds": (I, [I, P, L, I, I, P, P]),

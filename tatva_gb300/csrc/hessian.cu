@@ -10,32 +10,30 @@
 // Jc is computed here from element tangents instead of C full HVPs:
 //   Jc[i, c] = sum_e sum_{(b,k) in e : color(dof(b,k)) = c} K_e[(a,i), (b,k)]
 // which equals sum_{j: color j = c} H[i, j] because every element-local dof pair is
-// inside the pattern.  Each thread owns one (element, node a) row block; elements
-// are processed one element colour per launch (no two elements of a launch share a
-// node), so the read-modify-write of Jc rows is race-free and its order is fixed.
+// inside the pattern.  Node-centric: a thread owns one node's V rows of Jc and adds the
+// row blocks of the node's incident (element, corner) pairs in incidence order
+// (ascending element): deterministic, no atomics, no colouring of the elements.  With
+// a distance-2 colouring each colour occurs at most once per row, so a row is a dense
+// vector over the colours; the thread accumulates it in shared memory and the CTA
+// writes its consecutive nodes' rows as one contiguous, coalesced block of Jc.
 #include "tg_common.cuh"
 #include "tg_dispatch.cuh"
 #include "tg_materials.cuh"
 
 namespace tg {
 
+// Row block K_e[(a, i), (b, k)] (i, k < V, b < NN) of element e's tangent at u,
+// acc[i][b V + k]; nid: the element's nodes
 template <int ET, int MAT, class T>
-__global__ void compressed_hessian_kernel(const T* __restrict__ coords,
-                                          const int32_t* __restrict__ conn,
-                                          const T* __restrict__ u, T p0, T p1,
-                                          const T* __restrict__ eparam,
-                                          const int32_t* __restrict__ order, int n_in_color,
-                                          const int32_t* __restrict__ dof_colors, int n_colors,
-                                          T* __restrict__ Jc) {
+__device__ __forceinline__ void element_row_block(
+    const T* __restrict__ coords, const int32_t* __restrict__ conn, const T* __restrict__ u,
+    T p0, T p1, const T* __restrict__ eparam, int64_t e, int a,
+    T (&acc)[Law<MAT, Elem<ET>::D, T>::V][Elem<ET>::NN * Law<MAT, Elem<ET>::D, T>::V],
+    int (&nid)[Elem<ET>::NN]) {
   using E = Elem<ET>;
   using L = Law<MAT, E::D, T>;
   constexpr int NN = E::NN, D = E::D, V = L::V;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= n_in_color * NN) return;
-  const int a = tid % NN;
-  const int64_t e = __ldg(order + tid / NN);
   T X[NN][D], U[NN][V];
-  int nid[NN];
 #pragma unroll
   for (int b = 0; b < NN; ++b) {
     nid[b] = __ldg(conn + e * NN + b);
@@ -45,7 +43,6 @@ __global__ void compressed_hessian_kernel(const T* __restrict__ coords,
     for (int i = 0; i < V; ++i) U[b][i] = L::LINEAR ? T(0) : u[(int64_t)nid[b] * V + i];
   }
   const L law(eparam ? eparam[e] : p0, p1);
-  T acc[V][NN * V];
 #pragma unroll
   for (int i = 0; i < V; ++i)
 #pragma unroll
@@ -94,20 +91,61 @@ __global__ void compressed_hessian_kernel(const T* __restrict__ coords,
         }
       }
   }
-  int na = nid[0];
+}
+
+// Thread t of the CTA owns node n0 + t.  ACC_SMEM: its V x C row block sits in shared
+// memory at row t (stride V C + 1 words: conflict-free for the CTA's row-major write);
+// otherwise (too many colours for shared memory) it accumulates in its own rows of
+// Jc, which the caller zeroed.
+template <int ET, int MAT, class T, bool ACC_SMEM>
+__global__ void compressed_hessian_kernel(const T* __restrict__ coords,
+                                          const int32_t* __restrict__ conn,
+                                          const T* __restrict__ u, T p0, T p1,
+                                          const T* __restrict__ eparam, int64_t n_nodes,
+                                          const int32_t* __restrict__ inc_ptr,
+                                          const int32_t* __restrict__ inc_idx,
+                                          const int32_t* __restrict__ dof_colors, int n_colors,
+                                          T* __restrict__ Jc) {
+  using E = Elem<ET>;
+  using L = Law<MAT, E::D, T>;
+  constexpr int NN = E::NN, V = L::V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int row_words = V * n_colors;
+  const int stride = row_words + 1;
+  const int64_t n0 = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t n = n0 + threadIdx.x;
+  T* acc_row = ACC_SMEM ? sm + (int64_t)threadIdx.x * stride : Jc + n * row_words;
+  if (ACC_SMEM)
+    for (int k = 0; k < row_words; ++k) acc_row[k] = T(0);
+  if (n < n_nodes) {
+    for (int j = __ldg(inc_ptr + n); j < __ldg(inc_ptr + n + 1); ++j) {
+      const int ea = __ldg(inc_idx + j);
+      const int64_t e = ea / NN;
+      const int a = ea - (int)(e * NN);
+      T rb[V][NN * V];
+      int nid[NN];
+      element_row_block<ET, MAT, T>(coords, conn, u, p0, p1, eparam, e, a, rb, nid);
 #pragma unroll
-  for (int b = 1; b < NN; ++b)
-    if (b == a) na = nid[b];
+      for (int b = 0; b < NN; ++b)
 #pragma unroll
-  for (int i = 0; i < V; ++i) {
-    const int64_t row = (int64_t)na * V + i;
+        for (int k = 0; k < V; ++k) {
+          const int col = __ldg(dof_colors + (int64_t)nid[b] * V + k);
 #pragma unroll
-    for (int b = 0; b < NN; ++b)
-#pragma unroll
-      for (int k = 0; k < V; ++k) {
-        const int col = __ldg(dof_colors + (int64_t)nid[b] * V + k);
-        Jc[row * n_colors + col] += acc[i][b * V + k];
-      }
+          for (int i = 0; i < V; ++i) acc_row[i * n_colors + col] += rb[i][b * V + k];
+        }
+    }
+  }
+  if (ACC_SMEM) {
+    __syncthreads();
+    // rows of nodes n0 .. n0 + blockDim.x - 1 are one contiguous block of Jc
+    const int64_t rows_here = (n_nodes - n0) < (int64_t)blockDim.x ? (n_nodes - n0) : blockDim.x;
+    const int64_t total = rows_here * row_words;
+    T* out = Jc + n0 * row_words;
+    for (int64_t k = threadIdx.x; k < total; k += blockDim.x) {
+      const int t = (int)(k / row_words);
+      out[k] = sm[(int64_t)t * stride + (k - (int64_t)t * row_words)];
+    }
   }
 }
 
@@ -175,15 +213,21 @@ using namespace tg;
 
 extern "C" int tg_compressed_hessian(int elem, int prec, const tg_material* mat,
                                      const void* coords, int64_t n_nodes, const int32_t* conn,
-                                     int64_t n_elems, const void* u, const int32_t* elem_order,
-                                     const int32_t* elem_color_ptr_host, int n_elem_colors,
-                                     const int32_t* dof_colors, int n_colors, void* Jc,
-                                     void* stream) {
+                                     int64_t n_elems, const void* u, const int32_t* inc_ptr,
+                                     const int32_t* inc_idx, const int32_t* dof_colors,
+                                     int n_colors, void* Jc, void* stream) {
   TG_TRY(check_ptr(mat, "mat"));
   TG_TRY(check_sizes(n_elems, n_nodes, 1));
   TG_TRY(check_ptr(Jc, "Jc"));
   if (n_colors <= 0) return set_error(TG_ERR_VALUE, "n_colors must be positive");
-  if (n_elem_colors < 0) return set_error(TG_ERR_VALUE, "n_elem_colors must be >= 0");
+  if (n_nodes == 0) return TG_OK;
+  TG_TRY(check_ptr(inc_ptr, "inc_ptr"));
+  if (n_elems > 0) {
+    TG_TRY(check_ptr(coords, "coords"));
+    TG_TRY(check_ptr(conn, "conn"));
+    TG_TRY(check_ptr(inc_idx, "inc_idx"));
+    TG_TRY(check_ptr(dof_colors, "dof_colors"));
+  }
   cudaStream_t st = as_stream(stream);
   return dispatch_elem(elem, [&](auto et) -> int {
     constexpr int ET = decltype(et)::value;
@@ -195,28 +239,46 @@ extern "C" int tg_compressed_hessian(int elem, int prec, const tg_material* mat,
         return dispatch_prec(prec, [&](auto t) -> int {
           using T = decltype(t);
           constexpr int V = LawDims<MAT, Elem<ET>::D>::V;
-          const int64_t total = n_nodes * V * (int64_t)n_colors;
-          fill_kernel<T><<<grid_for(total, 256), 256, 0, st>>>((T*)Jc, total, T(0));
-          TG_TRY(launch_check("tg_compressed_hessian: zero"));
-          if (n_elems == 0) return TG_OK;
-          TG_TRY(check_ptr(coords, "coords"));
-          TG_TRY(check_ptr(conn, "conn"));
-          TG_TRY(check_ptr(elem_order, "elem_order"));
-          TG_TRY(check_ptr(elem_color_ptr_host, "elem_color_ptr"));
-          TG_TRY(check_ptr(dof_colors, "dof_colors"));
-          if (!Law<MAT, Elem<ET>::D, T>::LINEAR) TG_TRY(check_ptr(u, "u"));
-          for (int c = 0; c < n_elem_colors; ++c) {
-            const int k0 = elem_color_ptr_host[c], k1 = elem_color_ptr_host[c + 1];
-            const int cnt = k1 - k0;
-            if (cnt <= 0) continue;
-            compressed_hessian_kernel<ET, MAT, T>
-                <<<grid_for((int64_t)cnt * Elem<ET>::NN, 128), 128, 0, st>>>(
-                    (const T*)coords, conn, (const T*)u, (T)mat->p0, (T)mat->p1,
-                    (const T*)mat->elem_param, elem_order + k0, cnt, dof_colors, n_colors,
-                    (T*)Jc);
-            TG_TRY(launch_check("tg_compressed_hessian"));
+          if (!Law<MAT, Elem<ET>::D, T>::LINEAR && n_elems > 0) TG_TRY(check_ptr(u, "u"));
+          // threads per CTA (a multiple of 32, <= 128): the most resident threads per
+          // SM that shared memory allows (each thread holds one node's row block)
+          const size_t row_bytes = ((size_t)V * n_colors + 1) * sizeof(T);
+          int dev = 0, sm_bytes = 0, cta_bytes = 0;
+          TG_TRY(cuda_check(cudaGetDevice(&dev), "tg_compressed_hessian: device"));
+          TG_TRY(cuda_check(cudaDeviceGetAttribute(&sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev),
+                            "tg_compressed_hessian: shared memory per SM"));
+          TG_TRY(cuda_check(cudaDeviceGetAttribute(&cta_bytes, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+                            "tg_compressed_hessian: shared memory per CTA"));
+          int nt = 0, best = 0;
+          for (int cand = 128; cand >= 32; cand -= 32) {
+            const size_t need = (size_t)cand * row_bytes;
+            if (need > (size_t)cta_bytes) continue;
+            const int resident = (int)((size_t)sm_bytes / (need + 1024)) * cand;
+            if (resident > best) {
+              best = resident;
+              nt = cand;
+            }
           }
-          return TG_OK;
+          if (nt == 0) nt = 32;
+          const unsigned grid = (unsigned)((n_nodes + nt - 1) / nt);
+          if (best > 0) {
+            const size_t smem = (size_t)nt * row_bytes;
+            auto kern = compressed_hessian_kernel<ET, MAT, T, true>;
+            TG_TRY(cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem),
+                              "tg_compressed_hessian: shared memory"));
+            kern<<<grid, nt, smem, st>>>((const T*)coords, conn, (const T*)u, (T)mat->p0,
+                                         (T)mat->p1, (const T*)mat->elem_param, n_nodes, inc_ptr,
+                                         inc_idx, dof_colors, n_colors, (T*)Jc);
+          } else {
+            const int64_t total = n_nodes * V * (int64_t)n_colors;
+            fill_kernel<T><<<grid_for(total, 256), 256, 0, st>>>((T*)Jc, total, T(0));
+            compressed_hessian_kernel<ET, MAT, T, false><<<grid, 32, 0, st>>>(
+                (const T*)coords, conn, (const T*)u, (T)mat->p0, (T)mat->p1,
+                (const T*)mat->elem_param, n_nodes, inc_ptr, inc_idx, dof_colors, n_colors,
+                (T*)Jc);
+          }
+          return launch_check("tg_compressed_hessian");
         });
       }
     });

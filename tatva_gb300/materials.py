@@ -199,14 +199,13 @@ class Energy:
         (tatva/sparse/base.py:230-270), from element tangents."""
         dtype = dtype or u.dtype
         uf = self._flat(u).to(dtype)
-        order, cptr, nec = self.element_colors()
+        ip, ii = self.op.incidence()
         Jc = torch.empty((self.n_dofs, n_colors), dtype=dtype, device=uf.device)
         m = self.material(dtype)
-        cptr_c = np.ascontiguousarray(cptr, dtype=np.int32)
         _lib.call("tg_compressed_hessian", self.op.element.tg_id, prec_of(dtype), ctypes.byref(m),
                   ptr(self.op.coords_as(dtype)), self.op.n_nodes, ptr(self.op.mesh.elements),
-                  self.op.n_elements, ptr(uf), ptr(order), cptr_c.ctypes.data, nec,
-                  ptr(colors), int(n_colors), ptr(Jc), stream())
+                  self.op.n_elements, ptr(uf), ptr(ip), ptr(ii), ptr(colors), int(n_colors),
+                  ptr(Jc), stream())
         return Jc
 
     def operator_desc(self, u, fixed=None, dtype=torch.float64):

@@ -213,11 +213,14 @@ __global__ void __launch_bounds__(GR_THREADS, 2)
     const double* x = S->x;
     if (b < P.n_boundary_ctas)
       grid_boundary<double, TG_MODE_HVP, MASK_NODE, true, EPI_RESID>(
-          P, (int64_t)b * GR_THREADS, x, x, S->nmask, S->r64, reinterpret_cast<double*>(sm), dot,
+          P, (int64_t)b * GR_BNODES, x, x, S->nmask, S->r64, reinterpret_cast<double*>(sm), dot,
           S->b);
+    else if (b < P.n_boundary_ctas + P.n_xface_ctas)
+      grid_xface<double, TG_MODE_HVP, MASK_NODE, true, EPI_RESID>(
+          P, b - P.n_boundary_ctas, x, x, S->nmask, S->r64, sm, dot, S->b);
     else
       grid_interior<double, TG_MODE_HVP, MASK_NODE, true, EPI_RESID>(
-          P, b - P.n_boundary_ctas, x, x, S->nmask, S->r64, sm, dot, S->b);
+          P, b - P.n_boundary_ctas - P.n_xface_ctas, x, x, S->nmask, S->r64, sm, dot, S->b);
   }
   double v[1] = {dot.value()};
   reslot(L, e, s, S, b, count, slots);
@@ -304,12 +307,15 @@ __global__ void __launch_bounds__(GR_THREADS, TG_GRID_MINB)
   {
     const float* p = S->p;
     if (b < P.n_boundary_ctas)
-      grid_boundary<float, TG_MODE_HVP, MASK_NODE, true>(P, (int64_t)b * GR_THREADS, p, p,
+      grid_boundary<float, TG_MODE_HVP, MASK_NODE, true>(P, (int64_t)b * GR_BNODES, p, p,
                                                          S->nmask, S->q,
                                                          reinterpret_cast<float*>(sm), dot);
+    else if (b < P.n_boundary_ctas + P.n_xface_ctas)
+      grid_xface<float, TG_MODE_HVP, MASK_NODE, true>(P, b - P.n_boundary_ctas, p, p, S->nmask,
+                                                      S->q, sm, dot);
     else
-      grid_interior<float, TG_MODE_HVP, MASK_NODE, true>(P, b - P.n_boundary_ctas, p, p, S->nmask,
-                                                         S->q, sm, dot);
+      grid_interior<float, TG_MODE_HVP, MASK_NODE, true>(
+          P, b - P.n_boundary_ctas - P.n_xface_ctas, p, p, S->nmask, S->q, sm, dot);
   }
   double v[1] = {dot.value()};
   reslot(L, e, s, S, b, count, slots);  // recomputed: not held in registers across the sweep

@@ -58,10 +58,13 @@ __global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
   // boundary CTAs first: they start with the first wave and overlap the interior tiles
   const int b = blockIdx.x;
   if (b < P.n_boundary_ctas) {
-    grid_boundary<T, MODE, MK, DOT>(P, (int64_t)b * GR_THREADS, in, vin, fixed, y,
+    grid_boundary<T, MODE, MK, DOT>(P, (int64_t)b * GR_BNODES, in, vin, fixed, y,
                                       reinterpret_cast<T*>(sm), dot);
+  } else if (b < P.n_boundary_ctas + P.n_xface_ctas) {
+    grid_xface<T, MODE, MK, DOT>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm, dot);
   } else {
-    grid_interior<T, MODE, MK, DOT>(P, b - P.n_boundary_ctas, in, vin, fixed, y, sm, dot);
+    grid_interior<T, MODE, MK, DOT>(P, b - P.n_boundary_ctas - P.n_xface_ctas, in, vin, fixed,
+                                    y, sm, dot);
   }
   if constexpr (DOT) {
     double v[1] = {dot.value()};

@@ -34,9 +34,10 @@
 //     nine 16-byte shared loads and ~90 FP operations, using the stencil's symmetries
 //     (in-plane sums grouped by |dx|, |dy| for the diagonal blocks; signed cross sums
 //     for the off-diagonal ones).
-//   * boundary CTAs: the nodes on the six faces, one per thread, as the sum over the
-//     cells that exist around the node of the element matrix (24 x 24, staged in
-//     shared memory) times the cell's input values.
+//   * boundary CTAs: the nodes of the z and y faces, one per thread, as the sum over
+//     the cells that exist around the node of the element matrix (24 x 24, staged in
+//     shared memory) times the cell's input values; the x faces in 16 x 16 patches
+//     whose two node columns next to the face are staged in shared memory first.
 // Every output is written once by the thread that owns it, in a fixed order: the
 // result is deterministic and needs no atomics, partial slots or second pass.
 #pragma once
@@ -64,6 +65,11 @@ namespace tg {
 constexpr int GR_TX = 32, GR_TY = TG_GRID_TY, GR_THREADS = GR_TX * GR_TY;
 constexpr int GR_PX = GR_TX + 2, GR_PY = GR_TY + 2, GR_PLANE = GR_PX * GR_PY;  // 340
 constexpr int GR_SLOTS = (GR_PLANE + GR_THREADS - 1) / GR_THREADS;            // 2
+constexpr int GR_BNODES = GR_THREADS;                 // z / y face nodes per CTA
+constexpr int GR_XT = 16;                             // x-face patch: GR_XT x GR_XT nodes
+constexpr int GR_XS = GR_XT + 2;                      // staged rows per axis (with halo)
+static_assert(GR_XT * GR_XT == GR_THREADS, "one x-face node per thread");
+static_assert(2 * GR_XS * GR_XS <= 2 * GR_PLANE, "x-face staging fits the plane buffers");
 
 template <class T>
 struct GridCoef {
@@ -75,8 +81,10 @@ struct GridCoef {
   T ke[8][8][3][3];  // element matrix, corners cn, cm = lx + 2 ly + 4 lz
   int nx, ny, nz;    // nodes per axis
   int tiles_x, tiles_y, tiles_z, tz;  // interior tiling: tz planes per tile
-  int n_boundary_ctas;
-  int64_t n_boundary;
+  int n_boundary_ctas;   // z and y face nodes, one per thread
+  int xt_y, xt_z;        // x-face patches per face along y and z
+  int n_xface_ctas;      // 2 xt_y xt_z
+  int64_t n_boundary;    // z and y face nodes
 };
 
 template <class T>
@@ -378,37 +386,14 @@ __device__ __forceinline__ void boundary_node(int64_t t, int nx, int ny, int nz,
   z = 1 + (int)(r / (ny - 2));
 }
 
-template <class T, int MODE, int MK, bool DOT, int EPI = EPI_PLAIN>
-__device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restrict__ in,
-                              const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
-                              T* __restrict__ y, T* ke, DotAcc<T>& dot,
-                              const T* __restrict__ bres = nullptr) {
-  for (int i = threadIdx.x; i < 8 * 8 * 9; i += blockDim.x) ke[i] = (&P.ke[0][0][0][0])[i];
-  __syncthreads();
-  const int64_t t = t0 + threadIdx.x;
-  if (t >= P.n_boundary) return;
-  const int nx = P.nx, ny = P.ny, nz = P.nz;
-  int x, yy, z;
-  boundary_node(t, nx, ny, nz, x, yy, z);
-  T acc[3] = {T(0), T(0), T(0)};
-  for (int o = 0; o < 8; ++o) {  // cell whose corner o is this node
-    const int ox = o & 1, oy = (o >> 1) & 1, oz = o >> 2;
-    const int cx = x - ox, cy = yy - oy, cz = z - oz;
-    if (cx < 0 || cy < 0 || cz < 0 || cx >= nx - 1 || cy >= ny - 1 || cz >= nz - 1) continue;
-    const T* kr = ke + o * 72;  // rows of corner o: [cm][a][b]
-#pragma unroll
-    for (int cm = 0; cm < 8; ++cm) {
-      const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
-                                                         (int64_t)ny * (cz + (cm >> 2)));
-      const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
-      const T v0 = (m & 1) ? T(0) : __ldg(in + 3 * g);
-      const T v1 = (m & 2) ? T(0) : __ldg(in + 3 * g + 1);
-      const T v2 = (m & 4) ? T(0) : __ldg(in + 3 * g + 2);
-      const T* k9 = kr + cm * 9;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) acc[a] = fma(k9[3 * a + 2], v2, fma(k9[3 * a + 1], v1, fma(k9[3 * a], v0, acc[a])));
-    }
-  }
+// Output of a face node: the Dirichlet rows, the residual epilogue and the dot.
+template <class T, int MODE, int MK, bool DOT, int EPI>
+__device__ __forceinline__ void grid_emit_node(int x, int yy, int z, int nx, int ny,
+                                               const T (&acc)[3], const T* __restrict__ in,
+                                               const T* __restrict__ vin,
+                                               const uint8_t* __restrict__ fixed,
+                                               T* __restrict__ y, DotAcc<T>& dot,
+                                               const T* __restrict__ bres) {
   const int64_t gn = x + (int64_t)nx * (yy + (int64_t)ny * z), base = 3 * gn;
   const int mn = mask_bits<MK>(fixed, gn);
 #pragma unroll
@@ -428,6 +413,103 @@ __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restr
     if constexpr (DOT) dot.add(pv, val);
   }
 }
+
+// Nodes of the z and y faces, one per thread: the sum over the cells that exist
+// around the node of the element matrix times the cell's input values.  Consecutive
+// threads are consecutive along x, so the corner loads coalesce.
+template <class T, int MODE, int MK, bool DOT, int EPI = EPI_PLAIN>
+__device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restrict__ in,
+                              const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
+                              T* __restrict__ y, T* ke, DotAcc<T>& dot,
+                              const T* __restrict__ bres = nullptr) {
+  for (int i = threadIdx.x; i < 8 * 8 * 9; i += blockDim.x) ke[i] = (&P.ke[0][0][0][0])[i];
+  __syncthreads();
+  const int64_t t = t0 + threadIdx.x;
+  if (t >= P.n_boundary) return;
+  const int nx = P.nx, ny = P.ny, nz = P.nz;
+  int x, yy, z;
+  boundary_node(t, nx, ny, nz, x, yy, z);
+  T acc[3] = {T(0), T(0), T(0)};
+  for (int o = 0; o < 8; ++o) {  // cell whose corner o is this node
+    const int cx = x - (o & 1), cy = yy - ((o >> 1) & 1), cz = z - (o >> 2);
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= nx - 1 || cy >= ny - 1 || cz >= nz - 1) continue;
+    const T* kr = ke + o * 72;  // rows of corner o: [cm][a][b]
+#pragma unroll
+    for (int cm = 0; cm < 8; ++cm) {
+      const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
+                                                         (int64_t)ny * (cz + (cm >> 2)));
+      const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
+      const T v0 = (m & 1) ? T(0) : __ldg(in + 3 * g);
+      const T v1 = (m & 2) ? T(0) : __ldg(in + 3 * g + 1);
+      const T v2 = (m & 4) ? T(0) : __ldg(in + 3 * g + 2);
+      const T* k9 = kr + cm * 9;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a] = fma(k9[3 * a + 2], v2, fma(k9[3 * a + 1], v1, fma(k9[3 * a], v0, acc[a])));
+    }
+  }
+  grid_emit_node<T, MODE, MK, DOT, EPI>(x, yy, z, nx, ny, acc, in, vin, fixed, y, dot, bres);
+}
+
+// Nodes of the two x faces (x = 0 and x = nx - 1, 1 <= y <= ny - 2, 1 <= z <= nz - 2),
+// a GR_XT x GR_XT patch (y, z) per CTA.  On these faces consecutive nodes are a grid
+// row apart, so per-thread corner loads would touch one cache line per thread; the CTA
+// instead stages the two node columns next to the face (x = 0, 1 or nx - 2, nx - 1)
+// of its patch and halo, row by row (contiguous 24-byte runs), masked on the way.
+// All four cells around such a node exist, so the element-matrix indices are
+// compile-time constants.
+template <class T, int MODE, int MK, bool DOT, int EPI = EPI_PLAIN>
+__device__ void grid_xface(const GridCoef<T>& P, int item, const T* __restrict__ in,
+                           const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
+                           T* __restrict__ y, typename Vec4<T>::type* sm, DotAcc<T>& dot,
+                           const T* __restrict__ bres = nullptr) {
+  using V4 = typename Vec4<T>::type;
+  const int nx = P.nx, ny = P.ny, nz = P.nz;
+  const int per_face = P.xt_y * P.xt_z;
+  const int face = item / per_face, rest = item - face * per_face;
+  const int ty = rest % P.xt_y, tz = rest / P.xt_y;
+  const int xb = face ? nx - 2 : 0;  // first of the two staged columns
+  const int y0 = 1 + ty * GR_XT, z0 = 1 + tz * GR_XT;
+  // slot s = 2 (rz GR_XS + ry) + col: node (xb + col, y0 - 1 + ry, z0 - 1 + rz)
+  for (int s = threadIdx.x; s < 2 * GR_XS * GR_XS; s += blockDim.x) {
+    const int col = s & 1, r = s >> 1;
+    const int gy = y0 - 1 + r % GR_XS, gz = z0 - 1 + r / GR_XS;
+    T v0 = T(0), v1 = T(0), v2 = T(0);
+    if (gy < ny && gz < nz) {
+      const int64_t g = (xb + col) + (int64_t)nx * (gy + (int64_t)ny * gz);
+      const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
+      v0 = (m & 1) ? T(0) : __ldg(in + 3 * g);
+      v1 = (m & 2) ? T(0) : __ldg(in + 3 * g + 1);
+      v2 = (m & 4) ? T(0) : __ldg(in + 3 * g + 2);
+    }
+    sm[s] = make4<T>(v0, v1, v2);
+  }
+  __syncthreads();
+  const int ly = threadIdx.x % GR_XT, lz = threadIdx.x / GR_XT;
+  const int yy = y0 + ly, z = z0 + lz;
+  if (yy > ny - 2 || z > nz - 2) return;
+  T acc[3] = {T(0), T(0), T(0)};
+  auto cells = [&](auto ox_c) {
+    constexpr int OX = decltype(ox_c)::value;  // the node is corner x-index OX of its cells
+#pragma unroll
+    for (int oyz = 0; oyz < 4; ++oyz) {
+      const int oy = oyz & 1, oz = oyz >> 1;
+      const int o = OX + 2 * oy + 4 * oz;
+#pragma unroll
+      for (int cm = 0; cm < 8; ++cm) {
+        const int cmx = cm & 1, cmy = (cm >> 1) & 1, cmz = cm >> 2;
+        const V4 v = sm[2 * ((lz + 1 - oz + cmz) * GR_XS + (ly + 1 - oy + cmy)) + cmx];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          acc[a] = fma(P.ke[o][cm][a][2], v.z, fma(P.ke[o][cm][a][1], v.y, fma(P.ke[o][cm][a][0], v.x, acc[a])));
+      }
+    }
+  };
+  if (face) cells(std::integral_constant<int, 1>{});
+  else cells(std::integral_constant<int, 0>{});
+  grid_emit_node<T, MODE, MK, DOT, EPI>(face ? nx - 1 : 0, yy, z, nx, ny, acc, in, vin, fixed, y,
+                                        dot, bres);
+}
+
 
 // ------------------------------------------------------------------------- host
 // Stencil coefficients and the element matrix from the spacings and Lame parameters,
@@ -535,12 +617,16 @@ static int64_t grid_setup_dims(const int32_t nodes[3], const double h[3], double
   }
   P.tiles_z = iz > 0 ? (iz + P.tz - 1) / P.tz : 0;
   const int64_t n_int = (int64_t)P.tiles_x * P.tiles_y * P.tiles_z;
-  P.n_boundary = (int64_t)nx * ny * nz - (int64_t)(ix > 0 ? ix : 0) * (iy > 0 ? iy : 0) *
-                                             (iz > 0 ? iz : 0);
-  const int64_t n_bnd_ctas = (P.n_boundary + GR_THREADS - 1) / GR_THREADS;
-  if (n_int + n_bnd_ctas > 0x7fffffff) return -1;
+  // the z and y faces (thread per node), then the x faces (patches)
+  P.n_boundary = 2 * (int64_t)nx * ny + 2 * (int64_t)nx * (nz > 2 ? nz - 2 : 0);
+  const int64_t n_bnd_ctas = (P.n_boundary + GR_BNODES - 1) / GR_BNODES;
+  P.xt_y = iy > 0 ? (iy + GR_XT - 1) / GR_XT : 0;
+  P.xt_z = iz > 0 ? (iz + GR_XT - 1) / GR_XT : 0;
+  const int64_t n_x_ctas = 2 * (int64_t)P.xt_y * P.xt_z;
+  if (n_int + n_bnd_ctas + n_x_ctas > 0x7fffffff) return -1;
   P.n_boundary_ctas = (int)n_bnd_ctas;
-  return n_int + n_bnd_ctas;
+  P.n_xface_ctas = (int)n_x_ctas;
+  return n_int + n_bnd_ctas + n_x_ctas;
 }
 
 // The same for a structured-brick plan (tg_grid_detect's nodes and spacings).

@@ -162,3 +162,50 @@ def test_engine_reports_a_spent_refinement_budget(cuda):
     items = [_brick_problem(cuda, (9, 5, 7), (1.8, 0.5, 1.4), 1.3, 0.25, 0)]
     [(x, (status, its, outer, rr))] = _engine_solve(cuda, items, max_outer=1)
     assert status == _lib.TG_ERR_NOT_CONVERGED and outer == 1 and 1e-10 < rr < 1e-2
+
+
+def test_engine_rejects_bad_admissions_and_a_full_batch(cuda):
+    """Host-side checks of the C ABI: workspace size and alignment, brick size, a full
+    batch (64 slots), and the poll buffer length; the batch stays usable after each."""
+    bt = serving.BrickBatch(cuda)
+    st = torch.cuda.Stream(device=cuda)
+    nodes = (3, 3, 3)
+    wsb = int(_lib.lib().tg_brick_workspace_bytes((ctypes.c_int32 * 3)(*nodes)))
+    n = 3 * 27
+    b = torch.zeros(n, dtype=torch.float64, device=cuda)
+    keep = []
+
+    def req(ws_bytes=wsb, offset=0, nd=nodes):
+        x = torch.empty(n, dtype=torch.float64, device=cuda)
+        ws = torch.empty(wsb + 512, dtype=torch.uint8, device=cuda)
+        keep.append((x, ws))
+        r = _lib.BrickRequest()
+        r.nodes[:] = nd
+        r.h[:] = (0.5, 0.5, 0.5)
+        r.mu, r.lam = 1.0, 1.0
+        r.b, r.x, r.fixed = b.data_ptr(), x.data_ptr(), None
+        r.workspace, r.workspace_bytes = ws.data_ptr() + offset, ws_bytes
+        r.rtol, r.inner_rtol, r.max_outer, r.max_inner = 1e-10, 1e-4, 10, 1000
+        return r
+
+    with torch.cuda.stream(st):
+        with pytest.raises(RuntimeError):  # workspace too small
+            bt.admit(req(ws_bytes=wsb - 1), st)
+        with pytest.raises(ValueError):  # workspace not 256-byte aligned
+            bt.admit(req(offset=16), st)
+        with pytest.raises(ValueError):  # a brick needs 2 nodes per axis
+            bt.admit(req(nd=(1, 3, 3)), st)
+        slots = [bt.admit(req(), st) for _ in range(_lib.TG_BRICK_MAX_SLOTS)]
+        assert sorted(slots) == list(range(_lib.TG_BRICK_MAX_SLOTS))
+        with pytest.raises(ValueError):  # no free slot
+            bt.admit(req(), st)
+        short = (_lib.BrickState * 8)()
+        assert _lib.lib().tg_brick_poll(bt.handle, short, 8, st.cuda_stream) == _lib.TG_ERR_VALUE
+        # b = 0: every solve is converged at its first residual
+        bt.step(3, st)
+        states = bt.poll(st)
+        assert all(states[s].phase == _lib.TG_BRICK_DONE and states[s].status == 0 for s in slots)
+        states = bt.poll(st)
+        assert all(s.phase == _lib.TG_BRICK_FREE for s in states)
+        assert bt.admit(req(), st) == 0
+    bt.close()

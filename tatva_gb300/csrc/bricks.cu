@@ -85,11 +85,12 @@ __device__ __forceinline__ void chunk_of(int64_t n, int b, int nc, int64_t& i0, 
 }
 
 // true in the CTA of a slot's launch that arrives last (count CTAs); resets the counter
+// (thread 0 stored the CTA's partial and alone fences before arriving)
 __device__ __forceinline__ bool last_of(unsigned* ticket, int count) {
   __shared__ bool last;
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
+    __threadfence();
     const unsigned t = atomicAdd(ticket, 1u);
     last = (t == (unsigned)count - 1u);
     if (last) *ticket = 0u;
@@ -146,7 +147,9 @@ __device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
 
 // ------------------------------------------------------------------ admission
 // node mask, Jacobi inverse diagonal (FP64 sum of the element diagonals of the cells
-// around the node, rounded to FP32; fixed dofs: 1) and x = 0
+// around the node, rounded to FP32) and x = 0; on fixed dofs x = b (the identity rows of
+// the masked system) and a zero inverse diagonal, so that the inner CG's r, z, p and d
+// stay exactly zero there and its HVP masks only the output rows
 __global__ void __launch_bounds__(256) brick_admit_kernel(const __grid_constant__ Launch L,
                                                           BrickSlot* __restrict__ slots) {
   const int e = find_entry(L, blockIdx.x);
@@ -161,7 +164,7 @@ __global__ void __launch_bounds__(256) brick_admit_kernel(const __grid_constant_
     S->nmask[g] = (uint8_t)bits;
     const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = (int)(g / ((int64_t)nx * ny));
     for (int a = 0; a < 3; ++a) {
-      float dv = 1.0f;
+      float dv = 0.0f;
       if (!(bits >> a & 1)) {
         double sum = 0.0;
         for (int o = 0; o < 8; ++o) {  // cell whose corner o is this node
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(256) brick_admit_kernel(const __grid_constant_
         dv = 1.0f / (float)sum;
       }
       S->dinv[3 * g + a] = dv;
-      S->x[3 * g + a] = 0.0;
+      S->x[3 * g + a] = (bits >> a & 1) ? S->b[3 * g + a] : 0.0;
     }
   }
 }
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(GR_THREADS, 2)
   int b = blockIdx.x - L.off[e], count = L.off[e + 1] - L.off[e];
   copy_words(&P, &S->c64);
   __syncthreads();
-  DotAcc<double> dot;
+  GridDotAcc<double> dot;
   {
     const double* x = S->x;
     if (b < P.n_boundary_ctas)
@@ -303,18 +306,18 @@ __global__ void __launch_bounds__(GR_THREADS, TG_GRID_MINB)
   int b = blockIdx.x - L.off[e], count = L.off[e + 1] - L.off[e];
   copy_words(&P, &S->c32);
   __syncthreads();
-  DotAcc<float> dot;
+  GridDotAcc<float> dot;
   {
     const float* p = S->p;
     if (b < P.n_boundary_ctas)
-      grid_boundary<float, TG_MODE_HVP, MASK_NODE, true>(P, (int64_t)b * GR_BNODES, p, p,
-                                                         S->nmask, S->q,
-                                                         reinterpret_cast<float*>(sm), dot);
+      grid_boundary<float, TG_MODE_HVP, MASK_NODE_OUT, true>(P, (int64_t)b * GR_BNODES, p, p,
+                                                             S->nmask, S->q,
+                                                             reinterpret_cast<float*>(sm), dot);
     else if (b < P.n_boundary_ctas + P.n_xface_ctas)
-      grid_xface<float, TG_MODE_HVP, MASK_NODE, true>(P, b - P.n_boundary_ctas, p, p, S->nmask,
-                                                      S->q, sm, dot);
+      grid_xface<float, TG_MODE_HVP, MASK_NODE_OUT, true>(P, b - P.n_boundary_ctas, p, p,
+                                                          S->nmask, S->q, sm, dot);
     else
-      grid_interior<float, TG_MODE_HVP, MASK_NODE, true>(
+      grid_interior<float, TG_MODE_HVP, MASK_NODE_OUT, true>(
           P, b - P.n_boundary_ctas - P.n_xface_ctas, p, p, S->nmask, S->q, sm, dot);
   }
   double v[1] = {dot.value()};

@@ -54,7 +54,10 @@ __global__ void __launch_bounds__(GR_THREADS, sizeof(T) == 4 ? TG_GRID_MINB : 2)
                    T* __restrict__ y, const GridDot D) {
   using V4 = typename Vec4<T>::type;
   __shared__ V4 sm[2 * GR_PLANE];
-  DotAcc<T> dot;
+  if constexpr (DOT) {
+    if (D.scal[SCAL_DONE] != 0.0) return;  // the CG converged earlier in this block
+  }
+  GridDotAcc<T> dot;
   // boundary CTAs first: they start with the first wave and overlap the interior tiles
   const int b = blockIdx.x;
   if (b < P.n_boundary_ctas) {
@@ -122,6 +125,36 @@ int64_t grid_cg_ctas(const tg_block_plan* plan) {
   return grid_setup<float>(plan, 1.0, 1.0, P);
 }
 
+// The grid CG's handling of fixed dofs: x = b there (the identity rows of the masked
+// system) and a zero inverse diagonal, so that z, p and the updates of x and r are
+// exactly zero on them and the HVP of p needs no input mask.
+template <class T>
+__global__ void grid_cg_fixed_kernel(int64_t n_nodes, const uint8_t* __restrict__ nmask,
+                                     const T* __restrict__ b, T* __restrict__ x,
+                                     T* __restrict__ dinv) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_nodes) return;
+  const int m = nmask[g];
+  if (!m) return;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (m >> d & 1) {
+      x[3 * g + d] = b[3 * g + d];
+      dinv[3 * g + d] = T(0);
+    }
+}
+
+int grid_cg_fixed(int prec, int64_t n_nodes, const uint8_t* nmask, const void* b, void* x,
+                  void* dinv, cudaStream_t st) {
+  if (prec == TG_F32)
+    grid_cg_fixed_kernel<float><<<grid_for(n_nodes, 256), 256, 0, st>>>(
+        n_nodes, nmask, (const float*)b, (float*)x, (float*)dinv);
+  else
+    grid_cg_fixed_kernel<double><<<grid_for(n_nodes, 256), 256, 0, st>>>(
+        n_nodes, nmask, (const double*)b, (double*)x, (double*)dinv);
+  return launch_check("grid CG fixed dofs");
+}
+
 int pack_node_mask(const uint8_t* fixed, int64_t n_nodes, uint8_t* out, cudaStream_t st) {
   pack_node_mask_kernel<<<grid_for(n_nodes, 256), 256, 0, st>>>(fixed, n_nodes, out);
   return launch_check("pack node mask");
@@ -137,8 +170,8 @@ int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double l
     if (n <= 0) return set_error(TG_ERR_VALUE, "grid CG: empty or too large grid");
     const GridDot D{scal, part, ticket};
     const T* in = (const T*)p;
-    if (node_mask)
-      grid_le_kernel<T, TG_MODE_HVP, MASK_NODE, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
+    if (node_mask)  // p is zero on the fixed dofs (grid_cg_fixed): only the rows are masked
+      grid_le_kernel<T, TG_MODE_HVP, MASK_NODE_OUT, true><<<(unsigned)n, GR_THREADS, 0, st>>>(
           P, in, in, node_mask, (T*)q, D);
     else
       grid_le_kernel<T, TG_MODE_HVP, MASK_NONE, true><<<(unsigned)n, GR_THREADS, 0, st>>>(

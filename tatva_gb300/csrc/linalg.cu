@@ -280,6 +280,8 @@ __global__ void cg_init_final_kernel(const double* __restrict__ part, double* __
     scal[SCAL_RZ] = out[0];
     scal[SCAL_RR] = out[1];
     scal[SCAL_FLAG] = 0.0;
+    scal[SCAL_DONE] = 0.0;
+    scal[SCAL_ITERS] = 0.0;
   }
 }
 
@@ -289,6 +291,7 @@ template <class T>
 __global__ void __launch_bounds__(DOT_THREADS)
     cg_pq_kernel(const T* __restrict__ p, const T* __restrict__ q, int64_t n,
                  double* __restrict__ part, double* __restrict__ scal, unsigned* ticket) {
+  if (scal[SCAL_DONE] != 0.0) return;
   int64_t i0, i1;
   chunk_range(n, i0, i1);
   const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
@@ -325,6 +328,7 @@ __global__ void __launch_bounds__(DOT_THREADS)
     cg_update_kernel(int64_t n, double* __restrict__ scal, T* __restrict__ x,
                      T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ q,
                      const T* __restrict__ dinv, double* __restrict__ part, unsigned* ticket) {
+  if (scal[SCAL_DONE] != 0.0) return;
   int64_t i0, i1;
   chunk_range(n, i0, i1);
   const int64_t iv = i0 + ((i1 - i0) & ~int64_t(3));
@@ -375,6 +379,8 @@ __global__ void __launch_bounds__(DOT_THREADS)
     scal[SCAL_BETA] = bad ? 0.0 : rz_new / scal[SCAL_RZ];
     if (!bad) scal[SCAL_RZ] = rz_new;
     scal[SCAL_RR] = out[1];
+    scal[SCAL_ITERS] += 1.0;
+    if (out[1] <= scal[SCAL_TOL2]) scal[SCAL_DONE] = 1.0;
   }
 }
 
@@ -382,6 +388,7 @@ __global__ void __launch_bounds__(DOT_THREADS)
 template <class T>
 __global__ void cg_p_kernel(int64_t n, const double* __restrict__ scal, const T* __restrict__ r,
                             const T* __restrict__ dinv, T* __restrict__ p) {
+  if (scal[SCAL_DONE] != 0.0) return;
   const int64_t i = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
   const T beta = (T)scal[SCAL_BETA];
   if (i + 3 < n) {
@@ -665,19 +672,24 @@ static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
   return b;
 }
 
-// dinv = 1/diag ; r = b - A x ; p = r dinv ; scal <- (rz, rr); arrival counters zeroed
+// dinv = 1/diag ; r = b - A x ; p = r dinv ; scal <- (rz, rr); arrival counters zeroed.
+// Grid CG with fixed dofs: x = b and dinv = 0 on them first (grid_cg_fixed), so r, z and
+// p stay exactly zero there and the iterations' HVP masks only its output rows.
 template <class T>
 static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* diag,
                       CgBuffers& B, cudaStream_t st) {
   const int64_t n = op_ndofs(op);
+  inv_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, diag, (T*)B.dinv);
+  if (B.nmask) {
+    TG_TRY(pack_node_mask(op->fixed, op->n_nodes, B.nmask, st));
+    TG_TRY(grid_cg_fixed(op->prec, op->n_nodes, B.nmask, bvec, x, B.dinv, st));
+  }
   TG_TRY(tg_operator_apply(op, x, B.r, B.apply_ws, B.apply_bytes, st));
   axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
-  inv_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, diag, (T*)B.dinv);
   cg_init_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, (const T*)B.r, (const T*)B.dinv,
                                                         (T*)B.p, B.part);
   cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
   TG_TRY(cuda_check(cudaMemsetAsync(B.ticket, 0, 2 * sizeof(unsigned), st), "cg: counters"));
-  if (B.nmask) TG_TRY(pack_node_mask(op->fixed, op->n_nodes, B.nmask, st));
   return launch_check("cg restart");
 }
 
@@ -714,6 +726,10 @@ static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag
                   int max_iter, int check_every, CgBuffers& B, cudaStream_t st, int* iters) {
   double h[SCAL_N];
   TG_TRY(cg_restart<T>(op, bvec, x, diag, B, st));
+  const double tol2 = tol_abs * tol_abs;  // the update kernel's stopping test
+  TG_TRY(cuda_check(cudaMemcpyAsync(B.scal + SCAL_TOL2, &tol2, sizeof(double),
+                                    cudaMemcpyHostToDevice, st),
+                    "cg: tolerance"));
   TG_TRY(read_scalars(B.scal, h, st));
   *iters = 0;
   if (!std::isfinite(h[SCAL_RR])) return set_error(TG_ERR_BREAKDOWN, "cg: non-finite residual");
@@ -723,8 +739,10 @@ static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag
   int& graph_len = B.graph_len;
   const bool can_capture = (st != nullptr) && (st != cudaStreamLegacy) && (st != cudaStreamPerThread);
   int rc = TG_OK;
+  bool done = false;
   while (*iters < max_iter) {
     const int k = (max_iter - *iters) < check_every ? (max_iter - *iters) : check_every;
+    const int before = *iters;
     if (can_capture && k == check_every) {
       if (!exec || graph_len != k) {
         cudaGraph_t graph;
@@ -748,17 +766,22 @@ static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag
       for (int i = 0; i < k && rc == TG_OK; ++i) rc = cg_iteration<T>(op, x, diag, B, st);
       if (rc != TG_OK) break;
     }
-    *iters += k;
     rc = read_scalars(B.scal, h, st);
     if (rc != TG_OK) break;
+    *iters = (int)h[SCAL_ITERS];  // iterations that ran (a converged block stops early)
     if (h[SCAL_FLAG] != 0.0 || !std::isfinite(h[SCAL_RR])) {
       rc = set_error(TG_ERR_BREAKDOWN, "cg: breakdown (p.Ap <= 0 or non-finite) after %d iterations", *iters);
       break;
     }
-    if (std::sqrt(h[SCAL_RR]) <= tol_abs) break;
+    done = h[SCAL_DONE] != 0.0 || std::sqrt(h[SCAL_RR]) <= tol_abs;
+    if (done) break;
+    if (*iters == before) {  // no iteration ran although the solve has not converged
+      rc = set_error(TG_ERR_BREAKDOWN, "cg: no progress after %d iterations", *iters);
+      break;
+    }
   }
   if (rc != TG_OK) return rc;
-  if (std::sqrt(h[SCAL_RR]) > tol_abs)
+  if (!done)
     return set_error(TG_ERR_NOT_CONVERGED, "cg: not converged in %d iterations", *iters);
   return TG_OK;
 }

@@ -9,8 +9,12 @@ namespace tg {
 
 constexpr int DOT_CHUNKS = 2048;
 constexpr int DOT_THREADS = 256;
+// SCAL_TOL2: the squared residual tolerance of the running CG; SCAL_DONE: set by the
+// update when |r|^2 <= SCAL_TOL2 (the iteration's launches then return at once, so a
+// captured block of iterations stops doing work when the solve has converged inside
+// it); SCAL_ITERS: iterations performed.  Slots 5 and 7: true-residual norms.
 constexpr int SCAL_RZ = 0, SCAL_PQ = 1, SCAL_ALPHA = 2, SCAL_BETA = 3, SCAL_RR = 4,
-              SCAL_FLAG = 6, SCAL_N = 8;
+              SCAL_FLAG = 6, SCAL_TOL2 = 8, SCAL_DONE = 9, SCAL_ITERS = 10, SCAL_N = 12;
 
 // ------------------------------------------------------------------ dot accumulators
 // FP32 vectors: each thread accumulates x_i y_i as an unevaluated pair (hi, lo) of
@@ -73,11 +77,13 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[K], double* __res
 // Called by every thread after thread 0 stored this CTA's partials: true in the CTA
 // that arrives last, which then sees every CTA's partials (read them with __ldcg).
 // That CTA resets the ticket for the next launch.  An arrival counter, no waiting.
+// Only thread 0's partial has to be visible before its arrival, so only thread 0
+// fences: a fence in every thread waited for all of the CTA's output stores.
 __device__ __forceinline__ bool last_cta(unsigned* ticket) {
   __shared__ bool last;
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
+    __threadfence();
     const unsigned t = atomicAdd(ticket, 1u);
     last = (t == gridDim.x - 1);
     if (last) *ticket = 0u;

@@ -111,7 +111,28 @@ __device__ __forceinline__ typename Vec4<T>::type make4(T a, T b, T c) {
 // Dirichlet masks: none, one byte per dof (the C ABI's `fixed`), or one byte per node
 // with bit d set when dof 3 n + d is fixed (packed once per solve by the CG, so that a
 // node's mask is one load instead of three)
-constexpr int MASK_NONE = 0, MASK_DOF = 1, MASK_NODE = 2;
+// MASK_NODE_OUT: the node byte applied to the output rows only -- for inputs that are
+// already zero on the fixed dofs (the CG's direction when the preconditioner is zero
+// there), so the staged loads need no mask.
+constexpr int MASK_NONE = 0, MASK_DOF = 1, MASK_NODE = 2, MASK_NODE_OUT = 3;
+
+// whether the launch masks its input values (the Dirichlet columns of an HVP)
+template <int MODE, int MK>
+__device__ __forceinline__ constexpr bool masks_input() {
+  return MODE == TG_MODE_HVP && MK != MASK_NONE && MK != MASK_NODE_OUT;
+}
+
+// p.q (or r.r) of a grid launch: per node the three products summed in T (FMAs), the
+// node sums accumulated in FP64, in a fixed order -- a few instructions per node where
+// the compensated float pair of the vector kernels costs about thirty.
+template <class T>
+struct GridDotAcc {
+  double v = 0.0;
+  __device__ __forceinline__ void add3(const T (&a)[3], const T (&b)[3]) {
+    v += (double)fma(a[2], b[2], fma(a[1], b[1], a[0] * b[0]));
+  }
+  __device__ __forceinline__ double value() const { return v; }
+};
 
 // Output of a launch: the operator applied (EPI_PLAIN; with DOT, p.q of input and
 // output), or the residual y = b - A x of a right-hand side b (EPI_RESID; with DOT,
@@ -124,7 +145,7 @@ __device__ __forceinline__ int mask_bits(const uint8_t* __restrict__ fixed, int6
   if constexpr (MK == MASK_DOF) {
     return (__ldg(fixed + 3 * g) != 0) | (__ldg(fixed + 3 * g + 1) != 0) << 1 |
            (__ldg(fixed + 3 * g + 2) != 0) << 2;
-  } else if constexpr (MK == MASK_NODE) {
+  } else if constexpr (MK == MASK_NODE || MK == MASK_NODE_OUT) {
     return __ldg(fixed + g);
   } else {
     return 0;
@@ -216,7 +237,7 @@ __device__ __forceinline__ void stencil_plane(const GridCoef<T>& P,
 template <class T, int MODE, int MK, bool DOT, int EPI = EPI_PLAIN>
 __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restrict__ in,
                               const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
-                              T* __restrict__ y, typename Vec4<T>::type* sm, DotAcc<T>& dot,
+                              T* __restrict__ y, typename Vec4<T>::type* sm, GridDotAcc<T>& dot,
                               const T* __restrict__ bres = nullptr) {
   using V4 = typename Vec4<T>::type;
   const int tid = threadIdx.x;
@@ -254,7 +275,7 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
       for (int d = 0; d < 3; ++d) r[k][d] = T(0);
       if (soff[k] >= 0 && p <= ze) {
         const int64_t g = soff[k] + plane_nodes * p;
-        if (MODE == TG_MODE_HVP) m[k] = mask_bits<MK>(fixed, g);
+        if (masks_input<MODE, MK>()) m[k] = mask_bits<MK>(fixed, g);
 #pragma unroll
         for (int d = 0; d < 3; ++d) r[k][d] = __ldg(in + 3 * g + d);
       }
@@ -289,6 +310,7 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
   auto emit = [&](int z, const T (&acc)[3], const T (&pc)[3], int m) {
     if (!own || z < zs || z >= ze) return;
     const int64_t g = x + (int64_t)nx * yy + plane_nodes * z, base = 3 * g;
+    T pvs[3], vals[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T val = acc[d], pv = pc[d];
@@ -301,8 +323,10 @@ __device__ void grid_interior(const GridCoef<T>& P, int item, const T* __restric
         pv = val;
       }
       y[base + d] = val;
-      if constexpr (DOT) dot.add(pv, val);
+      pvs[d] = pv;
+      vals[d] = val;
     }
+    if constexpr (DOT) dot.add3(pvs, vals);
   };
 
   V4* buf0 = sm;
@@ -392,10 +416,11 @@ __device__ __forceinline__ void grid_emit_node(int x, int yy, int z, int nx, int
                                                const T (&acc)[3], const T* __restrict__ in,
                                                const T* __restrict__ vin,
                                                const uint8_t* __restrict__ fixed,
-                                               T* __restrict__ y, DotAcc<T>& dot,
+                                               T* __restrict__ y, GridDotAcc<T>& dot,
                                                const T* __restrict__ bres) {
   const int64_t gn = x + (int64_t)nx * (yy + (int64_t)ny * z), base = 3 * gn;
   const int mn = mask_bits<MK>(fixed, gn);
+  T pvs[3], vals[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     T val = acc[d];
@@ -410,8 +435,10 @@ __device__ __forceinline__ void grid_emit_node(int x, int yy, int z, int nx, int
       pv = val;
     }
     y[base + d] = val;
-    if constexpr (DOT) dot.add(pv, val);
+    pvs[d] = pv;
+    vals[d] = val;
   }
+  if constexpr (DOT) dot.add3(pvs, vals);
 }
 
 // Nodes of the z and y faces, one per thread: the sum over the cells that exist
@@ -420,7 +447,7 @@ __device__ __forceinline__ void grid_emit_node(int x, int yy, int z, int nx, int
 template <class T, int MODE, int MK, bool DOT, int EPI = EPI_PLAIN>
 __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restrict__ in,
                               const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
-                              T* __restrict__ y, T* ke, DotAcc<T>& dot,
+                              T* __restrict__ y, T* ke, GridDotAcc<T>& dot,
                               const T* __restrict__ bres = nullptr) {
   for (int i = threadIdx.x; i < 8 * 8 * 9; i += blockDim.x) ke[i] = (&P.ke[0][0][0][0])[i];
   __syncthreads();
@@ -438,7 +465,7 @@ __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restr
     for (int cm = 0; cm < 8; ++cm) {
       const int64_t g = (cx + (cm & 1)) + (int64_t)nx * ((cy + ((cm >> 1) & 1)) +
                                                          (int64_t)ny * (cz + (cm >> 2)));
-      const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
+      const int m = masks_input<MODE, MK>() ? mask_bits<MK>(fixed, g) : 0;
       const T v0 = (m & 1) ? T(0) : __ldg(in + 3 * g);
       const T v1 = (m & 2) ? T(0) : __ldg(in + 3 * g + 1);
       const T v2 = (m & 4) ? T(0) : __ldg(in + 3 * g + 2);
@@ -460,7 +487,7 @@ __device__ void grid_boundary(const GridCoef<T>& P, int64_t t0, const T* __restr
 template <class T, int MODE, int MK, bool DOT, int EPI = EPI_PLAIN>
 __device__ void grid_xface(const GridCoef<T>& P, int item, const T* __restrict__ in,
                            const T* __restrict__ vin, const uint8_t* __restrict__ fixed,
-                           T* __restrict__ y, typename Vec4<T>::type* sm, DotAcc<T>& dot,
+                           T* __restrict__ y, typename Vec4<T>::type* sm, GridDotAcc<T>& dot,
                            const T* __restrict__ bres = nullptr) {
   using V4 = typename Vec4<T>::type;
   const int nx = P.nx, ny = P.ny, nz = P.nz;
@@ -476,7 +503,7 @@ __device__ void grid_xface(const GridCoef<T>& P, int item, const T* __restrict__
     T v0 = T(0), v1 = T(0), v2 = T(0);
     if (gy < ny && gz < nz) {
       const int64_t g = (xb + col) + (int64_t)nx * (gy + (int64_t)ny * gz);
-      const int m = (MODE == TG_MODE_HVP) ? mask_bits<MK>(fixed, g) : 0;
+      const int m = masks_input<MODE, MK>() ? mask_bits<MK>(fixed, g) : 0;
       v0 = (m & 1) ? T(0) : __ldg(in + 3 * g);
       v1 = (m & 2) ? T(0) : __ldg(in + 3 * g + 1);
       v2 = (m & 4) ? T(0) : __ldg(in + 3 * g + 2);

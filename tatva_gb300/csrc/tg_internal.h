@@ -31,5 +31,8 @@ int launch_grid_hvp_dot(const tg_block_plan* plan, int prec, double mu, double l
                         const void* p, const uint8_t* node_mask, void* q, double* scal,
                         double* part, unsigned* ticket, cudaStream_t st);
 int pack_node_mask(const uint8_t* fixed, int64_t n_nodes, uint8_t* out, cudaStream_t st);
+// x = b and dinv = 0 on the fixed dofs of a packed node mask (the grid CG)
+int grid_cg_fixed(int prec, int64_t n_nodes, const uint8_t* nmask, const void* b, void* x,
+                  void* dinv, cudaStream_t st);
 
 }  // namespace tg

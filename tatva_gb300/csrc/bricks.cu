@@ -51,7 +51,8 @@ struct BrickSlot {
   float *r, *d, *p, *q, *dinv;
   uint8_t* nmask;  // one byte per node, bit a: dof 3 n + a fixed
   double* part;
-  double rtol, tol2_inner;
+  double rtol, inner_rtol;
+  double tol2_inner;  // of the running inner solve (set at each refinement)
   int max_outer, max_inner;
   // written on the device
   double scal[SCAL_N];
@@ -248,6 +249,11 @@ __global__ void __launch_bounds__(GR_THREADS, 2)
       q.status = TG_ERR_NOT_CONVERGED;
     } else {
       S->s = rn;
+      // the next inner solve reduces |r| only as far as the target still requires
+      // (factor-2 margin), at least by inner_rtol
+      double itol = 0.5 * S->rtol * bn / rn;
+      itol = itol < S->inner_rtol ? S->inner_rtol : (itol > 0.5 ? 0.5 : itol);
+      S->tol2_inner = itol * itol;
     }
   }
 }
@@ -576,6 +582,7 @@ extern "C" int tg_brick_admit(tg_brick_batch* bt, const tg_brick_request* req, v
   h.nmask = (uint8_t*)take((size_t)h.n_nodes);
   h.part = (double*)take(brick_part_doubles(nd) * sizeof(double));
   h.rtol = req->rtol;
+  h.inner_rtol = req->inner_rtol;
   h.tol2_inner = req->inner_rtol * req->inner_rtol;
   h.max_outer = req->max_outer;
   h.max_inner = req->max_inner;

@@ -916,7 +916,11 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
     scale_down_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, r64, 1.0 / rn, r32);
     TG_TRY(cuda_check(cudaMemsetAsync(d32, 0, n * sizeof(float), st), "mixed: zero"));
     int it = 0;
-    const int irc = cg_run<float>(op32, r32, d32, diag32, inner_rtol, max_inner, check_every, B, st, &it);
+    // the inner solve needs to reduce |r| only as far as the target still requires
+    // (with a factor-2 margin): the last refinement is not solved to inner_rtol
+    double itol = 0.5 * rtol * bn / rn;
+    itol = itol < inner_rtol ? inner_rtol : (itol > 0.5 ? 0.5 : itol);
+    const int irc = cg_run<float>(op32, r32, d32, diag32, itol, max_inner, check_every, B, st, &it);
     total_inner += it;
     if (irc == TG_ERR_BREAKDOWN) { rc = irc; break; }
     if (irc != TG_OK && irc != TG_ERR_NOT_CONVERGED) { rc = irc; break; }

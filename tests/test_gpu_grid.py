@@ -203,3 +203,25 @@ def test_grid_cg_with_prescribed_values_on_fixed_dofs(cuda):
     for res in (r64, rmx):
         assert torch.equal(res.x[f], b[f])
         assert rel(res.x, ref.x) < 1e-8
+
+
+def test_cg_result_does_not_depend_on_the_check_interval(cuda):
+    """The stopping test runs on the device after every iteration (a converged block of
+    captured iterations stops working), so iteration counts are exact and the solution
+    is bitwise the same whatever the host's check interval."""
+    from tatva_gb300 import solvers
+
+    c, e = om.brick(12, 10, 8, lengths=(1.2, 1.0, 0.8))
+    op = Operator(Mesh(c, e, device=cuda), element.Hexahedron8())
+    en = materials.LinearElastic.from_young(op, 1.0, 0.3)
+    fixed = np.zeros(en.n_dofs, np.uint8)
+    fixed.reshape(-1, 3)[c[:, 0] == 0.0] = 1
+    fixed = torch.as_tensor(fixed, device=cuda)
+    b = torch.as_tensor(np.random.default_rng(4).standard_normal(en.n_dofs) * 1e-3, device=cuda)
+    b[fixed.bool()] = 0.0
+    runs = [solvers.cg(en, b, fixed=fixed, rtol=1e-10, check_every=k) for k in (4, 10, 50)]
+    assert all(r.converged for r in runs)
+    assert len({r.iterations for r in runs}) == 1
+    assert all(torch.equal(r.x, runs[0].x) for r in runs[1:])
+    mixed = [solvers.mixed_cg(en, b, fixed=fixed, rtol=1e-10, check_every=k) for k in (6, 50)]
+    assert mixed[0].iterations == mixed[1].iterations and torch.equal(mixed[0].x, mixed[1].x)

@@ -105,3 +105,16 @@ def test_node_block_spmv_argument_checks():
         _lib.check(L.tg_spmv_blocks3(_lib.TG_F32, 6, None, None, None, None, None, None, None))
     assert L.tg_spmv_blocks3(_lib.TG_F32, 0, None, None, None, None, None, None, None) == _lib.TG_OK
 
+
+
+def test_brick_workspace_bytes_is_a_host_query():
+    """The request engine's per-request workspace size (host arithmetic, no device):
+    FP64 residual, five FP32 vectors, the node mask and the partials, each 256-byte
+    aligned; zero for a brick with fewer than two nodes on an axis."""
+    L = _lib.lib()
+    q = lambda n: int(L.tg_brick_workspace_bytes((ctypes.c_int32 * 3)(*n)))
+    assert q((1, 3, 3)) == 0 and q((3, 3, 1)) == 0
+    small, big = q((3, 3, 3)), q((17, 17, 17))
+    assert small > 0 and big > small and small % 256 == 0 and big % 256 == 0
+    ndof = 3 * 17 ** 3
+    assert big >= 8 * ndof + 5 * 4 * ndof + 17 ** 3

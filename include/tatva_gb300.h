@@ -418,7 +418,10 @@ TG_API int tg_operator_apply(const tg_operator_desc* op, const void* x, void* y,
 /* Jacobi-preconditioned CG, all vectors of precision op->prec, scalars and dot
  * products in FP64 on the device.  Solves A x = b from the given x.  The loop runs
  * `check_every` iterations per CUDA graph replay between host convergence checks
- * and never exceeds max_iter.  b and x must be 16-byte aligned (vector loads and
+ * and never exceeds max_iter; the stopping test itself runs on the device after
+ * every iteration, so the result does not depend on check_every.  On a structured
+ * brick with a Dirichlet mask, x is set to b on the fixed dofs first (the identity
+ * rows of the masked system).  b and x must be 16-byte aligned (vector loads and
  * stores), else TG_ERR_VALUE.                                                  */
 TG_API size_t tg_cg_workspace_bytes(const tg_operator_desc* op);
 TG_API int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, const void* diag,

@@ -568,15 +568,26 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   }
   __syncthreads();
 
+  // Every thread computes one element of the current chunk of blockDim.x elements
+  // into registers (no barrier), then the chunk's results are added into shared
+  // memory one element colour at a time (elements of a colour share no node).  The
+  // elements are stored by colour, so the additions at every node come in the plan's
+  // colour order, as in a colour-by-colour sweep, while no thread idles through the
+  // element work of a small colour.
   const int e_base = p.blk_elem_ptr[b];
-  const int c_begin = p.blk_color_ptr[b];
+  const int ne = p.blk_elem_ptr[b + 1] - e_base;
   const int c_last = p.blk_color_ptr[b + 1] - 1;
-  for (int c = c_begin; c < c_last; ++c) {
-    const int e_end = e_base + p.color_ofs[c + 1];
-    for (int e = e_base + p.color_ofs[c] + threadIdx.x; e < e_end; e += blockDim.x) {
-      int lc[NPAD];
+  const int nt = blockDim.x;
+  int c_first = p.blk_color_ptr[b];  // first colour that still has elements at or after k0
+  for (int k0 = 0; k0 < ne; k0 += nt) {
+    const int k = k0 + threadIdx.x;
+    const bool act = k < ne;
+    int lc[NPAD];
+    T Y[NN][V];
+    if (act) {
+      const int e = e_base + k;
       load_lconn<NPAD>(p.lconn + (int64_t)e * NPAD, lc);
-      T X[NN][D], U[NN][V], W[NN][V], Y[NN][V];
+      T X[NN][D], U[NN][V], W[NN][V];
 #pragma unroll
       for (int a = 0; a < NN; ++a) {
 #pragma unroll
@@ -587,14 +598,23 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
           W[a][i] = C::NEED_W ? Ws[lc[a] * V + i] : T(0);
         }
       }
-      const T k0 = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
-      element_apply<ET, MAT, T, MODE, AFFINE>(k0, p1, X, U, W, Y);
-#pragma unroll
-      for (int a = 0; a < NN; ++a)
-#pragma unroll
-        for (int i = 0; i < V; ++i) Ys[lc[a] * V + i] += Y[a][i];
+      const T kp = eparam ? eparam[__ldg(p.elem_id + e)] : p0;
+      element_apply<ET, MAT, T, MODE, AFFINE>(kp, p1, X, U, W, Y);
     }
-    __syncthreads();
+    while (c_first < c_last && p.color_ofs[c_first + 1] <= k0) ++c_first;
+    for (int c = c_first; c < c_last; ++c) {
+      const int lo = max(p.color_ofs[c], k0);
+      const int hi = min(p.color_ofs[c + 1], k0 + nt);
+      if (lo >= k0 + nt) break;  // the same decision in every thread of the block
+      if (lo >= hi) continue;
+      if (act && k >= lo && k < hi) {
+#pragma unroll
+        for (int a = 0; a < NN; ++a)
+#pragma unroll
+          for (int i = 0; i < V; ++i) Ys[lc[a] * V + i] += Y[a][i];
+      }
+      __syncthreads();
+    }
   }
 
   for (int l = threadIdx.x; l < nl; l += blockDim.x) {

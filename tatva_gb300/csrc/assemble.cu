@@ -56,7 +56,10 @@ __device__ __forceinline__ void element_generic(
   for (int a = 0; a < NN; ++a)
 #pragma unroll
     for (int i = 0; i < V; ++i) Y[a][i] = T(0);
-#pragma unroll
+  // Hex8: the eight quadrature points run as a loop (the per-point constants are a
+  // few selects); unrolled, the Hex8 element held ~200 registers and two CTAs per SM
+  constexpr int QUNROLL = (E::Q > 4) ? 1 : E::Q;
+#pragma unroll QUNROLL
   for (int q = 0; q < E::Q; ++q) {
     T G[NN][D];
     const T wd = qp_geometry<ET, T>(q, X, G) * E::template w<T>(q);

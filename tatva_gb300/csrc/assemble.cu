@@ -34,6 +34,11 @@
 namespace tg {
 
 constexpr int APPLY_MAX_THREADS = 256;
+// nodes a thread stages (and writes back) per pass of the general block kernel; Tri3
+// keeps one: its element is so small that the staging registers would set the
+// occupancy
+template <int ET>
+constexpr int apply_sb() { return ET == TG_TRI3 ? 1 : 4; }
 
 
 
@@ -543,7 +548,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
                        T* __restrict__ partials, T p0, T p1, const T* __restrict__ eparam) {
   using C = ApplyCfg<ET, MAT, T, MODE>;
   using E = Elem<ET>;
-  constexpr int NN = E::NN, D = C::D, V = C::V, NPAD = E::NPAD;
+  constexpr int NN = E::NN, D = C::D, V = C::V, NPAD = E::NPAD, SB = apply_sb<ET>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* smem = reinterpret_cast<T*>(smem_raw);
 
@@ -556,17 +561,41 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   T* Ws = Us + (C::NEED_U ? nl8 * V : 0);
   T* Ys = Ws + (C::NEED_W ? nl8 * V : 0);
 
-  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    const int64_t g = __ldg(p.lnode_gid + n0 + l);
-    const int q = __ldg(p.lnode_smem + n0 + l);
+  // staging: SB nodes per thread and pass, every node's global id loaded
+  // before any of the gathers that depend on it
+  for (int l0 = threadIdx.x; l0 < nl; l0 += SB * blockDim.x) {
+    int64_t g[SB];
+    int q[SB];
 #pragma unroll
-    for (int d = 0; d < D; ++d) Xs[q * D + d] = coords[g * D + d];
+    for (int k = 0; k < SB; ++k) {
+      const int l = l0 + k * blockDim.x;
+      g[k] = (l < nl) ? (int64_t)__ldg(p.lnode_gid + n0 + l) : -1;
+      q[k] = (l < nl) ? __ldg(p.lnode_smem + n0 + l) : 0;
+    }
+    T xv[SB][D], uv[SB][V], wv[SB][V];
 #pragma unroll
-    for (int i = 0; i < V; ++i) {
-      const int64_t dof = g * V + i;
-      if constexpr (C::NEED_U) Us[q * V + i] = u[dof];
-      if constexpr (C::NEED_W) Ws[q * V + i] = (fixed && fixed[dof]) ? T(0) : v[dof];
-      Ys[q * V + i] = T(0);
+    for (int k = 0; k < SB; ++k) {
+      if (g[k] < 0) continue;
+#pragma unroll
+      for (int d = 0; d < D; ++d) xv[k][d] = coords[g[k] * D + d];
+#pragma unroll
+      for (int i = 0; i < V; ++i) {
+        const int64_t dof = g[k] * V + i;
+        if constexpr (C::NEED_U) uv[k][i] = u[dof];
+        if constexpr (C::NEED_W) wv[k][i] = (fixed && fixed[dof]) ? T(0) : v[dof];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < SB; ++k) {
+      if (g[k] < 0) continue;
+#pragma unroll
+      for (int d = 0; d < D; ++d) Xs[q[k] * D + d] = xv[k][d];
+#pragma unroll
+      for (int i = 0; i < V; ++i) {
+        if constexpr (C::NEED_U) Us[q[k] * V + i] = uv[k][i];
+        if constexpr (C::NEED_W) Ws[q[k] * V + i] = wv[k][i];
+        Ys[q[k] * V + i] = T(0);
+      }
     }
   }
   __syncthreads();
@@ -582,14 +611,17 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   const int c_last = p.blk_color_ptr[b + 1] - 1;
   const int nt = blockDim.x;
   int c_first = p.blk_color_ptr[b];  // first colour that still has elements at or after k0
+  LconnRaw<NPAD> next;  // the row of this thread's element in the next chunk
+  if ((int)threadIdx.x < ne) next.load(p.lconn + (int64_t)(e_base + threadIdx.x) * NPAD);
   for (int k0 = 0; k0 < ne; k0 += nt) {
     const int k = k0 + threadIdx.x;
     const bool act = k < ne;
     int lc[NPAD];
     T Y[NN][V];
+    if (act) next.unpack(lc);
+    if (k + nt < ne) next.load(p.lconn + (int64_t)(e_base + k + nt) * NPAD);
     if (act) {
       const int e = e_base + k;
-      load_lconn<NPAD>(p.lconn + (int64_t)e * NPAD, lc);
       T X[NN][D], U[NN][V], W[NN][V];
 #pragma unroll
       for (int a = 0; a < NN; ++a) {
@@ -620,22 +652,35 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
     }
   }
 
-  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-    const int64_t g = __ldg(p.lnode_gid + n0 + l);
-    const int slot = __ldg(p.lnode_slot + n0 + l);
-    const int q = __ldg(p.lnode_smem + n0 + l);
-    if (slot < 0) {
+  // write-back: owned-alone nodes to y, shared nodes to their partial slot; the ids of
+  // SB nodes are loaded before their stores
+  for (int l0 = threadIdx.x; l0 < nl; l0 += SB * blockDim.x) {
+    int64_t g[SB];
+    int slot[SB], q[SB];
 #pragma unroll
-      for (int i = 0; i < V; ++i) {
-        const int64_t dof = g * V + i;
-        T val = Ys[q * V + i];
-        if (fixed && fixed[dof])
-          val = (MODE == TG_MODE_HVP) ? v[dof] : (MODE == TG_MODE_DIAG ? T(1) : T(0));
-        y[dof] = val;
+    for (int k = 0; k < SB; ++k) {
+      const int l = l0 + k * blockDim.x;
+      const bool in = l < nl;
+      g[k] = in ? (int64_t)__ldg(p.lnode_gid + n0 + l) : -1;
+      slot[k] = in ? __ldg(p.lnode_slot + n0 + l) : 0;
+      q[k] = in ? __ldg(p.lnode_smem + n0 + l) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < SB; ++k) {
+      if (g[k] < 0) continue;
+      if (slot[k] < 0) {
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+          const int64_t dof = g[k] * V + i;
+          T val = Ys[q[k] * V + i];
+          if (fixed && fixed[dof])
+            val = (MODE == TG_MODE_HVP) ? v[dof] : (MODE == TG_MODE_DIAG ? T(1) : T(0));
+          y[dof] = val;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < V; ++i) partials[(int64_t)slot[k] * V + i] = Ys[q[k] * V + i];
       }
-    } else {
-#pragma unroll
-      for (int i = 0; i < V; ++i) partials[(int64_t)slot * V + i] = Ys[q * V + i];
     }
   }
 }

@@ -212,4 +212,30 @@ __device__ __forceinline__ void load_lconn<8>(const uint16_t* __restrict__ p, in
   l[4] = v.z & 0xffff; l[5] = v.z >> 16; l[6] = v.w & 0xffff; l[7] = v.w >> 16;
 }
 
+// The packed row as loaded (one 8- or 16-byte load), for a load issued well before
+// the row is unpacked (the next chunk's row, fetched while this chunk computes).
+template <int NPAD>
+struct LconnRaw;
+template <>
+struct LconnRaw<4> {
+  uint2 v;
+  __device__ __forceinline__ void load(const uint16_t* __restrict__ p) {
+    v = __ldg(reinterpret_cast<const uint2*>(p));
+  }
+  __device__ __forceinline__ void unpack(int (&l)[4]) const {
+    l[0] = v.x & 0xffff; l[1] = v.x >> 16; l[2] = v.y & 0xffff; l[3] = v.y >> 16;
+  }
+};
+template <>
+struct LconnRaw<8> {
+  uint4 v;
+  __device__ __forceinline__ void load(const uint16_t* __restrict__ p) {
+    v = __ldg(reinterpret_cast<const uint4*>(p));
+  }
+  __device__ __forceinline__ void unpack(int (&l)[8]) const {
+    l[0] = v.x & 0xffff; l[1] = v.x >> 16; l[2] = v.y & 0xffff; l[3] = v.y >> 16;
+    l[4] = v.z & 0xffff; l[5] = v.z >> 16; l[6] = v.w & 0xffff; l[7] = v.w >> 16;
+  }
+};
+
 }  // namespace tg

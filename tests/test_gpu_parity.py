@@ -159,6 +159,39 @@ def test_hex_brick_affine_and_general(cuda, shape, jitter, kind):
             plan.grid = True
 
 
+@pytest.mark.parametrize("elem", ["tet4", "hex8"])
+def test_general_kernel_results_do_not_depend_on_the_cta_size(cuda, elem):
+    """The per-QP block kernel adds every node's element contributions in the plan's
+    colour order, whatever the number of threads per CTA: the same blocks run with
+    64, 128 and 256 threads give the same bits (FP32 and FP64), and the oracle's
+    values.  Kuhn tets and a jittered (non-affine) Hex8 brick, Neo-Hookean."""
+    if elem == "tet4":
+        m = Mesh.kuhn_box(7, 6, 5, device="cpu")
+        c, e = om.jitter_interior(m.coords_host(), 1.0 / 7, 0.2, seed=2), m.elements_host()
+        el, oel = element.Tetrahedron4(), oe.Tetrahedron4()
+    else:
+        c, e = om.brick(9, 8, 7)
+        c = om.jitter_interior(c, 1.0 / 9, 0.2, seed=3)
+        el, oel = element.Hexahedron8(), oe.Hexahedron8()
+    op = Operator(Mesh(c, e, device=cuda), el)
+    oo = oop.OracleOperator(c, e, oel)
+    en, law = materials.NeoHookean(op, 1.0, 10.0), omat.NeoHookean(1.0, 10.0)
+    rng = np.random.default_rng(6)
+    n = en.n_dofs
+    u, v = 0.01 * rng.standard_normal(n), rng.standard_normal(n)
+    want = omat.hvp(oo, law, u, v)
+    for dtype, tol in ((torch.float64, F64_TOL), (torch.float32, 1e-4)):
+        out = []
+        for threads in (64, 128, 256):
+            plan = op.plan(96, 4096, threads)
+            assert plan.sizes["n_blocks"] > 1 and plan.sizes["n_affine_blocks"] == 0
+            en.use_plan(plan)
+            out.append(en.hvp(_t(u, cuda, dtype), _t(v, cuda, dtype)))
+        en.use_plan(None)
+        assert torch.equal(out[0], out[1]) and torch.equal(out[0], out[2]), dtype
+        assert rel(out[0], want) < tol, dtype
+
+
 def test_hex_box_geometry_path_is_bitwise_equal(cuda):
     """FP32 box kernel with the plan's precomputed edge terms (box_geom32) equals the
     kernel that derives them from staged coordinates, bit for bit; both match the

@@ -208,7 +208,8 @@ bool hex_block_lattice(const double* coords, const int32_t* conn,
   return true;
 }
 
-// Shared-memory slots of a block's local nodes.  Consecutive element positions run on
+// Shared-memory slots of a block's local nodes for the affine Hex8 kernels, whose node
+// records are 16 bytes (one vector access per node).  Consecutive element positions run on
 // consecutive threads, so every run of 8 positions is one quarter-warp: the nodes it
 // reads at one element corner should sit in distinct 16-byte bank quads (slot % 8).
 // The same holds for every run of 8 consecutive local nodes, which one warp
@@ -263,6 +264,73 @@ void bank_aware_slots(const std::vector<int32_t>& lc_sorted, int npe, int ne, in
   int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   slot.assign(nl, 0);
   for (int v = 0; v < nl; ++v) slot[v] = quad[v] + 8 * cnt[quad[v]]++;
+}
+
+// Shared-memory slots for the general block kernel, whose node records are scalar
+// words (word d of a node at slot * stride + d, stride 1-3 and odd for every 3-D
+// law): the 32 lanes of a warp are one wavefront, free of bank conflicts when their
+// slots differ modulo 32.  Groups are every run of 32 element positions at one
+// corner (one warp's load or add) and every run of 32 consecutive local nodes (one
+// warp's staging or write-back).  Greedy capacity-constrained 32-colouring, the nodes
+// in most groups first (ties in order of first use); class r holds the slots
+// r, r + 32, ... below 8 ceil(nl / 8), so the shared-memory bound does not change.
+void bank_aware_slots32(const std::vector<int32_t>& lc_sorted, int npe, int ne, int nl,
+                        std::vector<int32_t>& slot) {
+  constexpr int W = 32;
+  const int ng_e = ((ne + W - 1) / W) * npe, ng = ng_e + (nl + W - 1) / W;
+  std::vector<int32_t> gptr(ng + 1, 0), gidx;
+  gidx.reserve((size_t)ne * npe + nl);
+  int gi = 0;
+  for (int g0 = 0; g0 < ne; g0 += W)
+    for (int c = 0; c < npe; ++c, ++gi) {
+      for (int k = g0; k < std::min(ne, g0 + W); ++k) gidx.push_back(lc_sorted[(size_t)k * npe + c]);
+      gptr[gi + 1] = (int32_t)gidx.size();
+    }
+  for (int s0 = 0; s0 < nl; s0 += W, ++gi) {
+    for (int v = s0; v < std::min(nl, s0 + W); ++v) gidx.push_back(v);
+    gptr[gi + 1] = (int32_t)gidx.size();
+  }
+  std::vector<int32_t> nptr(nl + 1, 0), nidx(gidx.size());
+  for (int32_t v : gidx) nptr[v + 1]++;
+  for (int i = 0; i < nl; ++i) nptr[i + 1] += nptr[i];
+  {
+    std::vector<int32_t> pos(nptr.begin(), nptr.end() - 1);
+    for (int g = 0; g < ng; ++g)
+      for (int k = gptr[g]; k < gptr[g + 1]; ++k) nidx[pos[gidx[k]]++] = g;
+  }
+  std::vector<int32_t> order;
+  order.reserve(nl);
+  {
+    std::vector<char> seen(nl, 0);
+    for (int32_t v : gidx)
+      if (!seen[v]) { seen[v] = 1; order.push_back(v); }
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    return nptr[a + 1] - nptr[a] > nptr[b + 1] - nptr[b];
+  });
+  const int nl8 = (nl + 7) & ~7;
+  int cap[W], used[W] = {};
+  for (int r = 0; r < W; ++r) cap[r] = r < nl8 ? (nl8 - r + W - 1) / W : 0;
+  std::vector<int> cls(nl, -1);
+  // hist[g * W + r]: members of group g already placed in class r (a node listed twice
+  // in a group counts twice, as it would when the members were walked)
+  std::vector<int32_t> hist((size_t)ng * W, 0);
+  for (int32_t v : order) {
+    int cost[W] = {};
+    for (int k = nptr[v]; k < nptr[v + 1]; ++k) {
+      const int32_t* h = hist.data() + (size_t)nidx[k] * W;
+      for (int r = 0; r < W; ++r) cost[r] += h[r];
+    }
+    int best = -1;
+    for (int r = 0; r < W; ++r)
+      if (used[r] < cap[r] && (best < 0 || cost[r] < cost[best])) best = r;
+    cls[v] = best;
+    used[best]++;
+    for (int k = nptr[v]; k < nptr[v + 1]; ++k) hist[(size_t)nidx[k] * W + best]++;
+  }
+  int cnt[W] = {};
+  slot.assign(nl, 0);
+  for (int v = 0; v < nl; ++v) slot[v] = cls[v] + W * cnt[cls[v]]++;
 }
 
 }  // namespace
@@ -721,7 +789,12 @@ extern "C" int tg_plan_build(int elem, const int32_t* conn, int64_t n_elems, int
             lc_sorted[(size_t)r * npe + a] = lid[conn[(int64_t)e * npe + a]];
         }
         std::vector<int32_t> smem_slot;
-        bank_aware_slots(lc_sorted, npe, ne, (int)ids.size(), smem_slot);
+        // affine Hex8 blocks run the kernels with 16-byte node records, every other
+        // block the general kernel with scalar records
+        if (b < P->n_affine)
+          bank_aware_slots(lc_sorted, npe, ne, (int)ids.size(), smem_slot);
+        else
+          bank_aware_slots32(lc_sorted, npe, ne, (int)ids.size(), smem_slot);
         for (int32_t r = 0; r < ne; ++r) {
           const int32_t dst = e0 + r;
           for (int a = 0; a < npe; ++a)

@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(APPLY_MAX_THREADS)
   const T* fin = (MODE == TG_MODE_RESIDUAL) ? u : v;
   const int nt = blockDim.x;
 
-  // ---- stage the block's nodes (4 nodes per thread per round, independent loads)
+  // ---- stage the block's nodes (4 nodes per thread per pass, independent loads)
   for (int l0 = threadIdx.x; l0 < nl; l0 += 4 * nt) {
     int64_t g[4];
 #pragma unroll

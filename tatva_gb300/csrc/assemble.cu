@@ -8,10 +8,11 @@
 // gather).
 //
 // Determinism without float atomics: every CTA owns one block of spatially compact
-// elements, stages the block's nodes in shared memory, processes its elements colour
-// by colour (no two elements of a colour share a node, so the shared-memory adds do
-// not race), then writes the nodes it owns alone straight to y and the nodes shared
-// with other blocks to partial-sum slots.  A second kernel adds each shared node's
+// elements and stages the block's nodes in shared memory.  It computes a chunk of
+// elements (one per thread) into registers, then adds the chunk's results into shared
+// memory colour by colour (no two elements of a colour share a node, so the adds do
+// not race).  Last it writes the nodes it owns alone straight to y and the nodes
+// shared with other blocks to partial-sum slots.  A second kernel adds each shared node's
 // partials in the fixed slot order.  The summation order is fixed by the plan, so
 // the result is bitwise reproducible.
 //

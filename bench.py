@@ -444,11 +444,15 @@ def run_ours(args):
     outer = results[-1].outer
     # launches per mixed solve: per inner iteration 3 kernels on a structured brick (the
     # HVP with p.q, the update, the direction), else the HVP plus 3 CG kernels; per
-    # refinement the FP64 HVP, 3 residual/norm kernels, the scale-down and the CG restart
-    # (HVP + 4 kernels) and the update; 3 set-up kernels, and the Jacobi diagonal
+    # refinement the FP64 HVP, 3 residual/norm kernels, the scale-down, the inner
+    # residual (HVP + 2 kernels, + 2 for the packed Dirichlet mask on a brick), the
+    # direction (2 kernels at a restart, 3 at a reliable update) and the update; 3
+    # set-up kernels, and the Jacobi diagonal
     per_inner = 3 if plan.grid else hvp_launches + 3
+    resumes = max(outer - 1, 0) if args.inner_rtol >= 0.01 else 0
     launches_per_solve = (inner * per_inner + (outer + 1) * (hvp_launches + 3)
-                          + outer * (hvp_launches + 6) + 3 + hvp_launches)
+                          + outer * (hvp_launches + 6 + (2 if plan.grid else 0)) + resumes
+                          + 3 + hvp_launches)
 
     # ---- e2e through the public API: each step's own right-hand side (the traction
     # scaled per step) from pinned host memory, its solution back to pinned host memory
@@ -1036,7 +1040,8 @@ def main():
     ap.add_argument("--block-elems", type=int, default=0, help="plan when --autotune 0")
     ap.add_argument("--threads", type=int, default=256, help="plan when --autotune 0")
     ap.add_argument("--max-iter", type=int, default=20000)
-    ap.add_argument("--inner-rtol", type=float, default=1e-4)
+    ap.add_argument("--inner-rtol", type=float, default=0.1,
+                    help="mixed solve: FP32 reduction between FP64 residual replacements")
     ap.add_argument("--check-every", type=int, default=50)
     ap.add_argument("--fp64-solves", type=int, default=2, help="timed FP64 solves (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

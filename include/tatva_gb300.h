@@ -431,7 +431,12 @@ TG_API int tg_cg_solve(const tg_operator_desc* op, const void* b, void* x, const
 /* Mixed precision: FP32 Jacobi-CG inner solves on op32 (FP32 HVP, FP64 dots),
  * FP64 iterative refinement with the true residual r = b - A64 x on op64.
  * b, x, diag64 are FP64; converges to ||b - A64 x|| <= rtol ||b||.  b must be
- * 16-byte aligned (vector loads), else TG_ERR_VALUE.                          */
+ * 16-byte aligned (vector loads), else TG_ERR_VALUE.  Each inner solve reduces its
+ * residual by inner_rtol (less on the last one).  inner_rtol >= 0.01: reliable
+ * updates, the inner CG keeps its search direction across the FP64 residual
+ * replacements (re-orthogonalised against the new residual; 0.1 recommended);
+ * smaller values restart the inner CG at every refinement.  max_outer bounds the
+ * replacements.                                                               */
 TG_API size_t tg_mixed_workspace_bytes(const tg_operator_desc* op64, const tg_operator_desc* op32);
 TG_API int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_desc* op32,
                    const double* b, double* x, const double* diag64, double rtol,

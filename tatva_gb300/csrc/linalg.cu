@@ -407,6 +407,86 @@ __global__ void cg_p_kernel(int64_t n, const double* __restrict__ scal, const T*
   }
 }
 
+// Reliable update of the inner recursion (the mixed solver, when the direction is
+// kept): r holds the new residual in the new unit, p the last direction in the old
+// unit, scale = |r_old| / |r_new| takes it over.  The direction is made orthogonal to
+// the new residual again (the recursive residual it was conjugated against has been
+// replaced) and extended as in a CG step:
+//   p <- dinv r + beta (scale p - c r),  c = scale (p.r) / (r.r),
+//   beta = (r.dinv r) / (rz_k scale^2),
+// rz_k being the r.z that the last direction was built from (rz / beta, as the update
+// kernel that stopped the recursion left them).  Pass 1: partials of p.r and r.r
+// (part2, two per chunk) and of r.dinv r (part1).
+template <class T>
+__global__ void __launch_bounds__(DOT_THREADS)
+    cg_resume_partial_kernel(int64_t n, const T* __restrict__ r, const T* __restrict__ dinv,
+                             const T* __restrict__ p, double* __restrict__ part2,
+                             double* __restrict__ part1) {
+  int64_t i0, i1;
+  chunk_range(n, i0, i1);
+  DotAcc<T> apr, arr, arz;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += DOT_THREADS) {
+    const T ri = r[i];
+    apr.add(p[i], ri);
+    arr.add(ri, ri);
+    arz.add(ri, ri * dinv[i]);
+  }
+  double v[3] = {apr.value(), arr.value(), arz.value()};
+  __shared__ double out[3];
+  block_reduce_store<3>(v, out);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    part2[2 * blockIdx.x] = out[0];
+    part2[2 * blockIdx.x + 1] = out[1];
+    part1[blockIdx.x] = out[2];
+  }
+}
+
+// the chunk partials added in a fixed order; coef = {beta scale, -beta c}.  A direction
+// that cannot be continued (no usable rz_k, a zero or non-finite product) gives beta =
+// 0, i.e. p = dinv r, the restart of the recursion.
+__global__ void cg_resume_final_kernel(const double* __restrict__ part2,
+                                       const double* __restrict__ part1, int nchunks,
+                                       double scale, double* __restrict__ scal,
+                                       double* __restrict__ coef) {
+  double w[3] = {0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nchunks; b += DOT_THREADS) {
+    w[0] += part2[2 * b];
+    w[1] += part2[2 * b + 1];
+    w[2] += part1[b];
+  }
+  __shared__ double out[3];
+  block_reduce_store<3>(w, out);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double pr = out[0], rr = out[1], rz = out[2];
+    const double beta_k = scal[SCAL_BETA];
+    const double rz_k = beta_k > 0.0 ? scal[SCAL_RZ] / beta_k : 0.0;
+    const bool ok = rz_k > 0.0 && isfinite(rz_k) && rr > 0.0 && rz > 0.0 && isfinite(pr) &&
+                    isfinite(rz) && scale > 0.0 && isfinite(scale);
+    const double beta = ok ? rz / (rz_k * scale * scale) : 0.0;
+    const double c = ok ? scale * pr / rr : 0.0;
+    coef[0] = beta * scale;
+    coef[1] = -beta * c;
+    scal[SCAL_RZ] = rz;
+    scal[SCAL_RR] = rr;
+    scal[SCAL_FLAG] = 0.0;
+    scal[SCAL_DONE] = 0.0;
+    scal[SCAL_ITERS] = 0.0;
+  }
+}
+
+template <class T>
+__global__ void cg_resume_p_kernel(int64_t n, const double* __restrict__ coef,
+                                   const T* __restrict__ r, const T* __restrict__ dinv,
+                                   T* __restrict__ p) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T a = (T)coef[0], c = (T)coef[1];
+  const T ri = r[i];
+  p[i] = ri * dinv[i] + a * p[i] + c * ri;
+}
+
 // out = (T)(r64 / |r64|) and x += |r64| d, the scale and its reciprocal passed in
 // (an FP64 square root or division per element costs more than the memory traffic on
 // this GPU's FP64 pipe)
@@ -675,12 +755,12 @@ static CgBuffers cg_carve(const tg_operator_desc* op, void* ws) {
   return b;
 }
 
-// dinv = 1/diag ; r = b - A x ; p = r dinv ; scal <- (rz, rr); arrival counters zeroed.
-// Grid CG with fixed dofs: x = b and dinv = 0 on them first (grid_cg_fixed), so r, z and
-// p stay exactly zero there and the iterations' HVP masks only its output rows.
+// dinv = 1/diag and the recursion's residual r = b - A x; the direction is left as it
+// is.  Grid CG with fixed dofs: x = b and dinv = 0 on them first (grid_cg_fixed), so r,
+// z and p stay exactly zero there and the iterations' HVP masks only its output rows.
 template <class T>
-static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* diag,
-                      CgBuffers& B, cudaStream_t st) {
+static int cg_residual(const tg_operator_desc* op, const T* bvec, T* x, const T* diag,
+                       CgBuffers& B, cudaStream_t st) {
   const int64_t n = op_ndofs(op);
   inv_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, diag, (T*)B.dinv);
   if (B.nmask) {
@@ -689,6 +769,15 @@ static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* 
   }
   TG_TRY(tg_operator_apply(op, x, B.r, B.apply_ws, B.apply_bytes, st));
   axpby_kernel<T><<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, bvec, -1.0, (T*)B.r);
+  return launch_check("cg residual");
+}
+
+// cg_residual, then p = r dinv ; scal <- (rz, rr); arrival counters zeroed
+template <class T>
+static int cg_restart(const tg_operator_desc* op, const T* bvec, T* x, const T* diag,
+                      CgBuffers& B, cudaStream_t st) {
+  const int64_t n = op_ndofs(op);
+  TG_TRY(cg_residual<T>(op, bvec, x, diag, B, st));
   cg_init_kernel<T><<<dot_chunks(n), DOT_THREADS, 0, st>>>(n, (const T*)B.r, (const T*)B.dinv,
                                                         (T*)B.p, B.part);
   cg_init_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, B.scal, dot_chunks(n));
@@ -724,11 +813,14 @@ static int read_scalars(const double* dev, double* host, cudaStream_t st) {
 
 // Runs CG from the current x until sqrt(rr) <= tol_abs (recursive residual) or the
 // iteration budget is spent.  Returns TG_OK, TG_ERR_NOT_CONVERGED or TG_ERR_BREAKDOWN.
+// resume: the recursion's residual, direction and scalars were set by the caller
+// (a reliable update) instead of a restart from x.
 template <class T>
 static int cg_run(const tg_operator_desc* op, const T* bvec, T* x, const T* diag, double tol_abs,
-                  int max_iter, int check_every, CgBuffers& B, cudaStream_t st, int* iters) {
+                  int max_iter, int check_every, CgBuffers& B, cudaStream_t st, int* iters,
+                  bool resume = false) {
   double h[SCAL_N];
-  TG_TRY(cg_restart<T>(op, bvec, x, diag, B, st));
+  if (!resume) TG_TRY(cg_restart<T>(op, bvec, x, diag, B, st));
   const double tol2 = tol_abs * tol_abs;  // the update kernel's stopping test
   TG_TRY(cuda_check(cudaMemcpyAsync(B.scal + SCAL_TOL2, &tol2, sizeof(double),
                                     cudaMemcpyHostToDevice, st),
@@ -899,8 +991,15 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
   dot_final_kernel<1><<<1, DOT_THREADS, 0, st>>>(part, sc + 1, dot_chunks(n));
   TG_TRY(launch_check("mixed: setup"));
   int total_inner = 0, outer = 0, rc = TG_OK;
-  double rn = 0.0, bn = 0.0;
+  double rn = 0.0, bn = 0.0, rn_prev = 0.0;
   double h[8];
+  // inner_rtol >= 0.01: reliable updates.  The inner recursion keeps its direction
+  // from one FP64 residual replacement to the next (re-orthogonalised against the new
+  // residual, cg_resume_*), so the Krylov information outlives the replacement; the
+  // replacements have to come often for that (every 10x reduction by default).
+  // Smaller inner_rtol: each refinement restarts the inner CG from d = 0.
+  const bool keep_direction = inner_rtol >= 0.01;
+  bool have_direction = false;
   for (;;) {
     // true residual r64 = b - A64 x in FP64
     TG_TRY(tg_operator_apply(op64, x, r64, aws64, ab64, st));
@@ -923,10 +1022,28 @@ extern "C" int tg_mixed_solve(const tg_operator_desc* op64, const tg_operator_de
     // (with a factor-2 margin): the last refinement is not solved to inner_rtol
     double itol = 0.5 * rtol * bn / rn;
     itol = itol < inner_rtol ? inner_rtol : (itol > 0.5 ? 0.5 : itol);
-    const int irc = cg_run<float>(op32, r32, d32, diag32, itol, max_inner, check_every, B, st, &it);
+    const bool resume = keep_direction && have_direction;
+    if (resume) {  // the recursion continues on the new residual (d = 0 again)
+      TG_TRY(cg_residual<float>(op32, r32, d32, diag32, B, st));
+      const int nc = dot_chunks(n);
+      cg_resume_partial_kernel<float><<<nc, DOT_THREADS, 0, st>>>(
+          n, (const float*)B.r, (const float*)B.dinv, (const float*)B.p, B.part, part);
+      cg_resume_final_kernel<<<1, DOT_THREADS, 0, st>>>(B.part, part, nc, rn_prev / rn, B.scal,
+                                                        sc + 2);
+      cg_resume_p_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(
+          n, sc + 2, (const float*)B.r, (const float*)B.dinv, (float*)B.p);
+      TG_TRY(cuda_check(cudaMemsetAsync(B.ticket, 0, 2 * sizeof(unsigned), st), "mixed: counters"));
+      TG_TRY(launch_check("mixed: reliable update"));
+    }
+    const int irc = cg_run<float>(op32, r32, d32, diag32, itol, max_inner, check_every, B, st,
+                                  &it, resume);
     total_inner += it;
     if (irc == TG_ERR_BREAKDOWN) { rc = irc; break; }
     if (irc != TG_OK && irc != TG_ERR_NOT_CONVERGED) { rc = irc; break; }
+    // the direction can be carried on only from a recursion that stopped in its update
+    // kernel (beta and rz of its last step are then in the scalars)
+    have_direction = irc == TG_OK && it > 0;
+    rn_prev = rn;
     // x += |r64| d
     scale_up_add_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(n, d32, rn, x);
     TG_TRY(launch_check("mixed: update"));

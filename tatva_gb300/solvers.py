@@ -104,10 +104,14 @@ def cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None, fixed
 
 
 def mixed_cg(energy, b: torch.Tensor, x0: torch.Tensor | None = None, *, u=None, fixed=None,
-             rtol: float = 1e-10, inner_rtol: float = 1e-4, max_outer: int = 50,
+             rtol: float = 1e-10, inner_rtol: float = 0.1, max_outer: int = 50,
              max_inner: int = 100000, check_every: int = 50,
              raise_on_fail: bool = True) -> SolveResult:
-    """FP32 inner CG + FP64 iterative refinement to ||b - A64 x|| <= rtol ||b||."""
+    """FP32 inner CG + FP64 iterative refinement to ||b - A64 x|| <= rtol ||b||.
+
+    ``inner_rtol`` is the FP32 residual reduction between two FP64 residual
+    replacements; from 0.01 up the inner CG keeps its search direction across them
+    (reliable updates), below it restarts at each refinement."""
     require_cuda(b)
     n = energy.n_dofs
     bb = aligned16(b.reshape(-1).to(torch.float64).contiguous())

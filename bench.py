@@ -7,7 +7,9 @@ nu = 0.3, clamped x = 0 face, uniform normal traction 1e-3 on x = 1.
 * step: one Jacobi-preconditioned CG solve of that system from x = 0 to
   ||b - A x|| <= 1e-10 ||b||, the residual evaluated in FP64.  The solve is the
   mixed-precision one of the public API (``solvers.mixed_cg``): FP32 matrix-free HVP
-  and inner CG vectors, FP64 true residual, refinement update and dot products.
+  and inner CG vectors, FP64 true residual, refinement update and dot products; the
+  inner CG keeps its direction across the FP64 residual replacements (reliable
+  updates, one per 10x reduction with the default ``--inner-rtol 0.1``).
   The L2 is flushed (256 MiB write) before every solve; the solve's own working set
   (about 280 MB of vectors) is larger than the L2 anyway.
 * value: solves per second over the K timed solves (CUDA events on the solver's
@@ -531,6 +533,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "precision": "FP32 HVP and inner CG vectors; FP64 true residual, refinement update "
                      "and every dot product; each solve stops at FP64 rel-res <= 1e-10",
+        "inner_rtol": args.inner_rtol,
         "data": "synthetic", "config": workload_config(n),
         "l2": "flushed before every solve (256 MiB write); solve working set > L2",
         "converged": conv, "rel_res": results[-1].rel_res, "inner_iterations": inner,
